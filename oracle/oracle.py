@@ -1,0 +1,222 @@
+"""Python side of the CPU oracle (test infrastructure only).
+
+Builds ``oracle/pyjac_oracle.c`` into ``oracle/_build/liboracle.so`` with gcc
+and exposes :class:`Oracle`, which evaluates species rates and the dense
+analytical Jacobian of a mechanism on the CPU from the reference-layout tables
+(``Mechanism.val``).  Also wraps the shim-compiled reference kernels in
+``oracle/_ref`` (:class:`RefKernels`) when they were built in this tree.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use this module, and only as the checker / the timed CPU
+baseline.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+SRC = os.path.join(HERE, "pyjac_oracle.c")
+HDR = os.path.join(HERE, "pyjac_oracle.h")
+
+
+def build(force=False, quiet=True):
+    os.makedirs(BUILD, exist_ok=True)
+    if (not force and os.path.exists(LIB) and
+            os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(HDR))):
+        return LIB
+    cmd = ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           SRC, "-o", LIB + ".tmp", "-lm"]
+    if not quiet:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+_I = ctypes.POINTER(ctypes.c_int)
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+class _OrcMech(ctypes.Structure):
+    _fields_ = [("ns", ctypes.c_int), ("nr", ctypes.c_int),
+                ("net_off", _I), ("net_spec", _I), ("net_nu", _I), ("nu_sum", _I),
+                ("rev_mask", _I),
+                ("rxn_simple", _I), ("rxn_plog", _I), ("rxn_cheb", _I), ("rxn_thd", _I),
+                ("rxn_fall", _I),
+                ("simple_type", _I), ("simple_A", _D), ("simple_b", _D), ("simple_Ta", _D),
+                ("plog_maxP", ctypes.c_int), ("plog_numP", _I), ("plog_params", _D),
+                ("n_plog", ctypes.c_int),
+                ("cheb_maxT", ctypes.c_int), ("cheb_maxP", ctypes.c_int), ("n_cheb", ctypes.c_int),
+                ("cheb_nT", _I), ("cheb_nP", _I), ("cheb_params", _D), ("cheb_Plim", _D),
+                ("cheb_Tlim", _D),
+                ("thd_type", _I), ("thd_off", _I), ("thd_spec", _I), ("thd_eff", _D),
+                ("fall_ftype", _I), ("fall_blend", _I), ("fall_type", _I),
+                ("fall_A", _D), ("fall_b", _D), ("fall_Ta", _D),
+                ("fall_troe", _I), ("fall_sri", _I),
+                ("troe_a", _D), ("troe_T1", _D), ("troe_T2", _D), ("troe_T3", _D),
+                ("sri_a", _D), ("sri_b", _D), ("sri_c", _D), ("sri_d", _D), ("sri_e", _D),
+                ("a_lo", _D), ("a_hi", _D), ("T_mid", _D), ("mw_post", _D)]
+
+
+def _offsets(counts):
+    counts = np.asarray(counts, dtype=np.int64)
+    return np.concatenate(([0], np.cumsum(counts))).astype(np.int32)
+
+
+class Oracle(object):
+    """CPU evaluation of species rates and the dense Jacobian (C order in/out)."""
+
+    def __init__(self, mech):
+        self._lib = ctypes.CDLL(build())
+        for fn in (self._lib.orc_species_rates, self._lib.orc_jacobian):
+            fn.restype = ctypes.c_int
+            fn.argtypes = [ctypes.POINTER(_OrcMech), ctypes.c_long, ctypes.c_int, _D, _D, _D,
+                           ctypes.c_int]
+        self.mech = mech
+        v = mech.val
+        Ns, Nr = v["Ns"], v["Nr"]
+        keep = self._keep = []
+
+        def I(a):
+            a = np.ascontiguousarray(np.asarray(a, dtype=np.int32).ravel())
+            if a.size == 0:
+                a = np.zeros(1, dtype=np.int32)
+            keep.append(a)
+            return a.ctypes.data_as(_I)
+
+        def D(a):
+            a = np.ascontiguousarray(np.asarray(a, dtype=np.float64).ravel())
+            if a.size == 0:
+                a = np.zeros(1)
+            keep.append(a)
+            return a.ctypes.data_as(_D)
+
+        def rxn_index(mp):
+            out = -np.ones(Nr, dtype=np.int32)
+            out[np.asarray(mp, dtype=np.int64)] = np.arange(len(mp))
+            return out
+
+        fall = v["fall"]
+        nfall = int(fall["num"])
+        fall_troe = -np.ones(max(nfall, 1), dtype=np.int32)
+        fall_troe[np.asarray(fall["troe"]["map"], dtype=np.int64)] = np.arange(fall["troe"]["num"])
+        fall_sri = -np.ones(max(nfall, 1), dtype=np.int32)
+        fall_sri[np.asarray(fall["sri"]["map"], dtype=np.int64)] = np.arange(fall["sri"]["num"])
+        rev_mask = rxn_index(v["rev"]["map"])
+        plog = v["plog"]
+        cheb = v["cheb"]
+        m = _OrcMech()
+        m.ns, m.nr = Ns, Nr
+        m.net_off = I(_offsets(v["net"]["num_reac_to_spec"]))
+        m.net_spec = I(v["net"]["reac_to_spec"])
+        m.net_nu = I(v["net"]["nu"])
+        m.nu_sum = I(v["net"]["nu_sum"])
+        m.rev_mask = I(rev_mask)
+        m.rxn_simple = I(rxn_index(v["simple"]["map"]))
+        m.rxn_plog = I(rxn_index(plog["map"]))
+        m.rxn_cheb = I(rxn_index(cheb["map"]))
+        m.rxn_thd = I(rxn_index(v["thd"]["map"]))
+        m.rxn_fall = I(rxn_index(fall["map"]))
+        m.simple_type = I(v["simple"]["type"])
+        m.simple_A = D(v["simple"]["A"])
+        m.simple_b = D(v["simple"]["b"])
+        m.simple_Ta = D(v["simple"]["Ta"])
+        m.n_plog = int(plog["num"])
+        m.plog_maxP = int(plog["max_P"] or 0)
+        m.plog_numP = I(plog["num_P"])
+        m.plog_params = D(plog["post_process"]["params"])
+        m.n_cheb = int(cheb["num"])
+        pp = np.asarray(cheb["post_process"]["params"])
+        m.cheb_maxT = int(pp.shape[1]) if m.n_cheb else 0
+        m.cheb_maxP = int(pp.shape[2]) if m.n_cheb else 0
+        m.cheb_nT = I(cheb["num_T"])
+        m.cheb_nP = I(cheb["num_P"])
+        m.cheb_params = D(pp)
+        m.cheb_Plim = D(cheb["post_process"]["Plim"])
+        m.cheb_Tlim = D(cheb["post_process"]["Tlim"])
+        m.thd_type = I(v["thd"]["type"])
+        m.thd_off = I(_offsets(v["thd"]["spec_num"]))
+        m.thd_spec = I(v["thd"]["spec"])
+        m.thd_eff = D(v["thd"]["eff"])
+        m.fall_ftype = I(fall["ftype"] if nfall else [])
+        m.fall_blend = I(fall["blend"])
+        m.fall_type = I(fall["type"])
+        m.fall_A = D(fall["A"])
+        m.fall_b = D(fall["b"])
+        m.fall_Ta = D(fall["Ta"])
+        m.fall_troe = I(fall_troe)
+        m.fall_sri = I(fall_sri)
+        for k in ("a", "T1", "T2", "T3"):
+            setattr(m, "troe_" + k, D(fall["troe"][k]))
+        for k in ("a", "b", "c", "d", "e"):
+            setattr(m, "sri_" + k, D(fall["sri"][k]))
+        m.a_lo = D(v["thermo"]["a_lo"])
+        m.a_hi = D(v["thermo"]["a_hi"])
+        m.T_mid = D(v["thermo"]["T_mid"])
+        m.mw_post = D(v["mw_post"])
+        self._m = m
+        self.nn = Ns + 1
+
+    def _call(self, fn, param, phi, out, conp, nthreads):
+        param = np.ascontiguousarray(param, dtype=np.float64)
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        rc = fn(ctypes.byref(self._m), phi.shape[0], int(bool(conp)), param.ctypes.data_as(_D),
+                phi.ctypes.data_as(_D), out.ctypes.data_as(_D), int(nthreads))
+        if rc != 0:
+            raise RuntimeError("oracle returned %d" % rc)
+        return out
+
+    def species_rates(self, param, phi, conp=True, nthreads=0):
+        """phi (n, NN) C order -> dphi (n, NN)."""
+        out = np.empty_like(np.asarray(phi, dtype=np.float64))
+        return self._call(self._lib.orc_species_rates, param, phi, out, conp, nthreads)
+
+    def jacobian(self, param, phi, conp=True, nthreads=0):
+        """phi (n, NN) C order -> dense jac (n, NN, NN), jac[i, row, col]."""
+        n = np.asarray(phi).shape[0]
+        out = np.empty((n, self.nn, self.nn))
+        return self._call(self._lib.orc_jacobian, param, phi, out, conp, nthreads)
+
+
+class RefKernels(object):
+    """The reference's shipped generated kernels, shim-compiled into oracle/_ref.
+
+    Available only where ``oracle/build_ref.py`` could compile them (it needs
+    the reference tree).  F order in and out, conp, hybrid rate spec.
+    """
+
+    def __init__(self, mech_name):
+        so = os.path.join(HERE, "_ref", "libref_%s.so" % mech_name)
+        if not os.path.exists(so):
+            raise FileNotFoundError(so)
+        self._lib = ctypes.CDLL(so)
+        ns, nn, js = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._lib.ref_info(ctypes.byref(ns), ctypes.byref(nn), ctypes.byref(js))
+        self.ns, self.nn, self.jac_size = ns.value, nn.value, js.value
+        for fn in (self._lib.ref_species_rates, self._lib.ref_jacobian):
+            fn.restype = ctypes.c_int
+            fn.argtypes = [ctypes.c_long, _D, _D, _D, ctypes.c_int]
+
+    @staticmethod
+    def available(mech_name):
+        return os.path.exists(os.path.join(HERE, "_ref", "libref_%s.so" % mech_name))
+
+    def species_rates_F(self, P, phi_F, nthreads=0):
+        n = P.shape[0]
+        out = np.zeros((self.nn, n))
+        self._lib.ref_species_rates(n, np.ascontiguousarray(P).ctypes.data_as(_D),
+                                    np.ascontiguousarray(phi_F).ctypes.data_as(_D),
+                                    out.ctypes.data_as(_D), int(nthreads))
+        return out
+
+    def jacobian_F(self, P, phi_F, nthreads=0):
+        n = P.shape[0]
+        out = np.zeros((self.jac_size, n))
+        self._lib.ref_jacobian(n, np.ascontiguousarray(P).ctypes.data_as(_D),
+                               np.ascontiguousarray(phi_F).ctypes.data_as(_D),
+                               out.ctypes.data_as(_D), int(nthreads))
+        return out
