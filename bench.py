@@ -1,0 +1,324 @@
+"""Benchmark: GRI-Mech 3.0 dense FP64 analytical Jacobians on one GB300.
+
+Workload (the headline configuration): GRI-Mech 3.0 (53 species, 325
+reactions), 1,048,576 seeded synthetic states (T ~ U(800, 2200) K,
+P log-uniform 1-25 atm, X ~ Dirichlet(0.5) floored at 1e-12, V = 1 m^3),
+constant pressure, F data order, dense 54 x 54 Jacobian.  One step = one
+Jacobian evaluation of all states (pjg_jacobian).  Inputs (432 MB) and outputs
+(24.9 GB) are larger than L2, so no flush is needed between steps.
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the reference's CPU
+implementation of the same path on the host cores instead: the shim-compiled
+shipped GRI kernels in oracle/_ref when they load here, else the C oracle
+(the CPU restatement of the reference) with OpenMP on all cores.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import importlib  # noqa: E402
+
+PKG = "pyjac-v2_gb300"
+METRIC = "GRI-30 FP64 Jacobians/s"
+UNIT = "Jacobians/s"
+
+# algorithmic HBM bytes per state: read phi (NN) + param, write NN^2 (dense)
+NN_GRI = 54
+
+
+def alg_bytes_per_state(nn, n_out):
+    return 8 * (nn + 1) + 8 * n_out
+
+
+def pkg(sub=None):
+    return importlib.import_module(PKG + ("." + sub if sub else ""))
+
+
+def load_gri():
+    return pkg().load_mechanism(os.path.join(ROOT, "data", "grimech30.inp"),
+                                os.path.join(ROOT, "data", "thermo30.dat"))
+
+
+class ClockSampler(object):
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_reference_run(mech, n_sample, steps, seed=1):
+    """Time the reference's CPU implementation: states/s and a description."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    orc = importlib.import_module("oracle")
+    states = pkg("states")
+    P, phi = states.draw_states(mech.n_species, n_sample, seed=seed, x_floor=1e-12)
+    threads = cpu_threads()
+    kind, fn = None, None
+    if orc.RefKernels.available("ch4"):
+        try:
+            ref = orc.RefKernels("ch4")
+            phiF = np.ascontiguousarray(phi.T)
+            kind = "reference"
+            desc = "reference shipped GRI-30 kernels (examples/opencl/ch4, sparse CCS), shim-compiled"
+
+            def fn():
+                ref.jacobian_F(P, phiF, nthreads=threads)
+        except OSError:
+            kind = None
+    if kind is None:
+        o = orc.Oracle(mech)
+        kind = "port"
+        desc = "C oracle (CPU restatement of the reference), dense Jacobian, OpenMP"
+
+        def fn():
+            o.jacobian(P, phi, conp=True, nthreads=threads)
+    fn()  # warm-up call, then timed calls (the reference's main times its second call)
+    ts = []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t0)
+    sec = float(np.mean(ts))
+    return {"value": n_sample / sec, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": "%d GRI-30 states per step, %s" % (n_sample, desc)}, sec
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    mech = load_gri()
+    n = args.cpu_sample
+    cb, sec = cpu_reference_run(mech, n, args.steps)
+    out = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "GRI-Mech 3.0 FP64 Jacobian, %d states per step on host cores" % n,
+                      "mechanism": "grimech30", "states": n, "conp": True},
+           "cpu_baseline": cb,
+           "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--states", type=int, default=1 << 20)
+    ap.add_argument("--format", default="full", choices=["full", "sparse"])
+    ap.add_argument("--order", default="F", choices=["C", "F"])
+    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = pkg("_lib")
+    api = pkg("api")
+    states = pkg("states")
+    mech = load_gri()
+    ev = api.Evaluator(mech)
+    n = args.states
+    nn = mech.nn
+    n_out = nn * nn if args.format == "full" else mech.jac_nnz()
+    P, phi = states.draw_states(mech.n_species, n, seed=1000 + rank, x_floor=1e-12)
+    x = np.ascontiguousarray(phi.T) if args.order == "F" else phi
+    tP = torch.from_numpy(P).to(dev)
+    tphi = torch.from_numpy(x).to(dev)
+    out = torch.empty(n * n_out, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        ev.jacobian(tP, tphi, order=args.order, conp=True, jac_format=args.format, out=out)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    fp64_peak = ctypes.c_double()
+    lib.check("pjg_fp64_peak", lib.load().pjg_fp64_peak(ctypes.byref(fp64_peak)))
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.launch_count()
+    lib.profile_begin()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    n_eval, eval_ms = lib.profile_end()
+    launches = lib.launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    clk = clocks.stop()
+    ms_step = ms / args.steps
+    value = world * n * args.steps / (ms * 1e-3)
+
+    # roofline of the dominant kernel (the fused Jacobian evaluation kernel)
+    bytes_step = alg_bytes_per_state(nn, n_out) * n
+    achieved = bytes_step * args.steps / (eval_ms * 1e-3) / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm_peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as fh:
+            hbm_peak = float(json.load(fh).get("hbm_gbs", hbm_peak))
+        peak_src = "measured"
+    flops_path = os.path.join(ROOT, "profiles", "fp64_ops_gri30_jacobian.json")
+    fp64 = {"peak": fp64_peak.value, "unit": "TFLOP/s",
+            "peak_source": "measured DFMA probe (pjg_fp64_peak)"}
+    if os.path.exists(flops_path):
+        with open(flops_path) as fh:
+            fl = json.load(fh)
+        key = "%s_%s" % (args.format, args.order)
+        if key in fl.get("flops_per_state", {}):
+            fps = fl["flops_per_state"][key]
+            ach = fps * n * args.steps / (eval_ms * 1e-3) / 1e12
+            fp64 = {"achieved": ach, "peak": fp64_peak.value, "unit": "TFLOP/s",
+                    "frac": ach / fp64_peak.value, "flops_per_state": fps,
+                    "peak_source": "measured DFMA probe (pjg_fp64_peak)"}
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None,
+                "peak_source": peak_src, "kernel": "eval_kernel<1> (fused Jacobian)",
+                "alg_bytes_per_state": alg_bytes_per_state(nn, n_out),
+                "eval_ms_per_step": eval_ms / args.steps, "eval_launches": n_eval,
+                "fp64": fp64}
+    traffic_path = os.path.join(ROOT, "profiles", "traffic_gri30_jacobian.json")
+    if os.path.exists(traffic_path):
+        with open(traffic_path) as fh:
+            tr = json.load(fh)
+        key = "%s_%s" % (args.format, args.order)
+        if key in tr.get("dram_bytes_per_state", {}):
+            roofline["traffic"] = tr["dram_bytes_per_state"][key] * n / max(1, n_eval // args.steps)
+
+    # end to end through the reference-facing kernel object, host buffers (pinned)
+    e2e = None
+    if not args.no_e2e:
+        mod = api.pywrap(mech, order=args.order, conp=True, jac_format=args.format)
+        jk = mod.PyJacobianKernel(n, 1)
+        hP = torch.from_numpy(P).pin_memory().numpy()
+        hphi = torch.from_numpy(x).pin_memory().numpy()
+        hjac = torch.empty(n * n_out, dtype=torch.float64, pin_memory=True).numpy()
+        jk(hP, hphi, hjac)
+        k2 = max(1, min(args.steps, 3))
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(k2):
+            jk(hP, hphi, hjac)
+        sec = (time.perf_counter() - t0) / k2
+        e2e = {"value": world * n / sec, "unit": UNIT,
+               "h2d_bytes_per_step": int(hP.nbytes + hphi.nbytes),
+               "d2h_bytes_per_step": int(hjac.nbytes), "steps": k2,
+               "path": "PyJacobianKernel(problem_size, work_size)(param, phi, jac), pinned host arrays"}
+        jk.close()
+        del hjac
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu, _ = cpu_reference_run(mech, args.cpu_sample, 1)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "GRI-Mech 3.0 %s FP64 Jacobian, %s order, %d states"
+                           % ("dense" if args.format == "full" else "sparse CCS/CRS", args.order, n),
+                           "mechanism": "grimech30 (53 species, 325 reactions)",
+                           "states": n, "order": args.order, "jac_format": args.format,
+                           "conp": True, "l2": "inputs 432 MB and outputs > L2; no flush"},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clk}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

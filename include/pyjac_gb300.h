@@ -1,0 +1,135 @@
+/*
+ * pyjac-v2_gb300 C ABI: batched species rates and analytical Jacobians of a
+ * chemical-kinetic mechanism on one GB300 (sm_103a), FP64 throughout.
+ *
+ * This ABI replaces the runtime boundary of pyJac-v2's generated code:
+ *   - the generated C++ kernel class (pyjac/kernel_utils/common/kernel.hpp.in:86-335,
+ *     kernel.cpp.in:539-633): Kernel(problem_size, work_size, do_not_compile),
+ *     resize(), operator()(double* param, double* phi, double* out),
+ *     requiredMemorySize(), numSpecies(), numReactions(), order();
+ *   - the generated device entry points species_rates(t, P_arr, phi, dphi, rwk)
+ *     and jacobian(t, P_arr, phi, jac, rwk)
+ *     (examples/opencl/ch4/species_rates.ocl:354, jacobian.ocl:1130) and their
+ *     lockstep drivers (pyjac/core/driver_kernels.py:321-367);
+ *   - the Cython wrapper's arrays, passed as &arr[0]
+ *     (pyjac/pywrap/pyjacob_wrapper.pyx.in:19-92).
+ *
+ * Data conventions are pyJac's (pyjac/core/array_creator.py:1938-2110):
+ *   phi  = (T, V or P, n_0 .. n_{Ns-2}) per state, NN = Ns + 1 entries;
+ *   param = P (constant pressure, conp) or V (constant volume);
+ *   dphi = d phi / dt;
+ *   order 'C': phi[i*NN + j], dense jac[i*NN*NN + row*NN + col],
+ *              sparse jac[i*nnz + p] in CRS order;
+ *   order 'F': phi[i + N*j],  dense jac[i + N*row + N*NN*col],
+ *              sparse jac[i + N*p] in CCS order.
+ *
+ * Every function returns 0 on success and a negative pjg_status on error; none
+ * aborts.  pjg_last_error() returns a thread-local description of the last
+ * error.  Functions taking a `stream` are asynchronous on that CUDA stream
+ * (cudaStream_t passed as void*; NULL = legacy default stream) and take
+ * device pointers; pjg_kernel_call takes host pointers and is synchronous,
+ * as the reference's operator() is.
+ */
+#ifndef PYJAC_GB300_H
+#define PYJAC_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum pjg_status {
+    PJG_OK = 0,
+    PJG_ERR_ARG = -1,        /* invalid argument (null pointer, bad size, bad enum) */
+    PJG_ERR_CUDA = -2,       /* a CUDA runtime call failed */
+    PJG_ERR_TABLES = -3,     /* inconsistent or unsupported mechanism tables */
+    PJG_ERR_UNSUPPORTED = -4 /* option combination not supported */
+};
+
+enum pjg_kind { PJG_SPECIES_RATES = 0, PJG_JACOBIAN = 1 };
+enum pjg_jac_format { PJG_JAC_FULL = 0, PJG_JAC_SPARSE = 1 };
+
+/* Host-side mechanism tables produced by the Python front end
+ * (pyjac-v2_gb300/pack.py).  All arrays are read during pjg_mech_create and
+ * may be freed afterwards.  Byte layouts are documented in
+ * pyjac-v2_gb300/csrc/pjg_tables.cuh. */
+typedef struct pjg_tables {
+    int32_t ns;              /* species, bath gas last */
+    int32_t nr;              /* reactions */
+    int32_t flags;           /* bit 0: mechanism has PLOG/Chebyshev (needs ln P) */
+    const void* rxn;         /* nr reaction records, 192 bytes each */
+    const double* species;   /* ns species records, 16 doubles each */
+    const int32_t* thd_spec; /* third-body species lists */
+    const double* thd_coef;  /* efficiency minus flag, aligned with thd_spec */
+    int32_t n_thd;           /* length of thd_spec / thd_coef */
+    const double* aux;       /* PLOG / Chebyshev parameter blocks */
+    int32_t n_aux;           /* length of aux in doubles */
+    /* Jacobian non-zero pattern (create_jacobian.py:235-282) */
+    int32_t nnz;
+    const int32_t* crs_row_ptr;  /* NN + 1 */
+    const int32_t* crs_col_ind;  /* nnz */
+    const int32_t* ccs_col_ptr;  /* NN + 1 */
+    const int32_t* ccs_row_ind;  /* nnz */
+} pjg_tables;
+
+typedef struct pjg_mech pjg_mech;
+typedef struct pjg_kernel pjg_kernel;
+
+/* Upload tables to the current CUDA device. */
+int pjg_mech_create(const pjg_tables* tables, pjg_mech** out);
+int pjg_mech_destroy(pjg_mech* mech);
+/* numSpecies() / numReactions() of kernel.hpp.in */
+int pjg_mech_info(const pjg_mech* mech, int32_t* ns, int32_t* nr, int32_t* nnz);
+
+/* Jacobian index arrays of kernel order: CRS (row_ptr, col_ind) for 'C',
+ * CCS (col_ptr, row_ind) for 'F' (create_jacobian.py:235-282).  ptr has NN+1
+ * entries, ind has nnz; either may be NULL to query only *nnz. */
+int pjg_jacobian_indices(const pjg_mech* mech, char order, int32_t* ptr, int32_t* ind,
+                         int32_t* nnz);
+
+/* Device-pointer entry points (asynchronous on `stream`).
+ * Replace the generated species_rates / jacobian drivers. */
+int pjg_species_rates(pjg_mech* mech, int64_t n, char order, int conp, const double* param,
+                      const double* phi, double* dphi, void* stream);
+int pjg_jacobian(pjg_mech* mech, int64_t n, char order, int conp, int jac_format,
+                 const double* param, const double* phi, double* jac, void* stream);
+/* Vector-Jacobian product out = J^T v (dense J of kernel order; v, out have NN
+ * entries per state in `order`).  No reference counterpart: the adjoint used
+ * by the torch wdot autograd.Function. */
+int pjg_vjp(pjg_mech* mech, int64_t n, char order, int conp, const double* param,
+            const double* phi, const double* v, double* out, void* stream);
+
+/* Kernel objects: the reference's Kernel class (kernel.hpp.in:86-335).
+ * problem_size = states per call; work_size is accepted for API
+ * compatibility (the reference's OpenMP thread / OpenCL group count) and
+ * ignored: the GPU kernels size their own grids.  Host pointers; each call
+ * copies inputs in, evaluates, copies outputs out and synchronises. */
+int pjg_kernel_create(pjg_mech* mech, int kind, size_t problem_size, size_t work_size,
+                      char order, int conp, int jac_format, pjg_kernel** out);
+int pjg_kernel_resize(pjg_kernel* k, size_t problem_size, size_t work_size);
+int pjg_kernel_call(pjg_kernel* k, const double* param, const double* phi, double* out);
+/* requiredMemorySize(): device bytes held by the kernel object */
+int pjg_kernel_required_memory(const pjg_kernel* k, size_t* bytes);
+int pjg_kernel_destroy(pjg_kernel* k);
+
+/* Copy the last error message of this thread into buf (always NUL-terminated). */
+int pjg_last_error(char* buf, size_t len);
+
+/* Instrumentation (no reference counterpart; the reference prints wall-clock
+ * timings from its generated main, kernel.cpp.in:645-712).
+ * pjg_launch_count: GPU kernel launches this library has issued so far.
+ * pjg_profile_begin / pjg_profile_end: record CUDA events around every launch
+ * of the evaluation kernels between the two calls; end synchronises those
+ * events and returns their number and summed duration in milliseconds. */
+int pjg_launch_count(int64_t* count);
+/* Measured dense FP64 FMA throughput of the current device in TFLOP/s (the
+ * denominator of the FP64 roofline; runs a ~10 ms probe kernel). */
+int pjg_fp64_peak(double* tflops);
+int pjg_profile_begin(void);
+int pjg_profile_end(int64_t* launches, double* total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -72,7 +72,7 @@ class Oracle(object):
 
     def __init__(self, mech):
         self._lib = ctypes.CDLL(build())
-        for fn in (self._lib.orc_species_rates, self._lib.orc_jacobian):
+        for fn in (self._lib.orc_species_rates, self._lib.orc_jacobian, self._lib.orc_rates_scale):
             fn.restype = ctypes.c_int
             fn.argtypes = [ctypes.POINTER(_OrcMech), ctypes.c_long, ctypes.c_int, _D, _D, _D,
                            ctypes.c_int]
@@ -174,6 +174,11 @@ class Oracle(object):
         """phi (n, NN) C order -> dphi (n, NN)."""
         out = np.empty_like(np.asarray(phi, dtype=np.float64))
         return self._call(self._lib.orc_species_rates, param, phi, out, conp, nthreads)
+
+    def rates_scale(self, param, phi, conp=True, nthreads=0):
+        """Per-entry cancellation scale of dphi (n, NN); see orc_rates_scale."""
+        out = np.empty_like(np.asarray(phi, dtype=np.float64))
+        return self._call(self._lib.orc_rates_scale, param, phi, out, conp, nthreads)
 
     def jacobian(self, param, phi, conp=True, nthreads=0):
         """phi (n, NN) C order -> dense jac (n, NN, NN), jac[i, row, col]."""

@@ -58,6 +58,7 @@ typedef struct ws {
     int n_fall, n_thd;
     double *conc, *kf, *kr, *kf_fall, *thd_conc, *Pr, *Fi, *Fcent, *Atroe, *Btroe;
     double *Xsri, *b, *pres_mod, *ropf, *ropr, *wdot, *h, *cp, *dcp, *db, *dphi;
+    double *gross, *scale; /* cancellation scale of wdot and of dphi (test metric only) */
 } ws;
 
 /* Arrhenius forms of rate_subs.py get_simple_arrhenius_rates (:2642-3023). */
@@ -293,7 +294,7 @@ static void eval_rates(const orc_mech* m, int conp, double param, const double* 
     }
     /* rates of progress (get_rop :1371-1509, get_rop_net :1170-1370) and
      * net production (get_spec_rates :1079-1167) */
-    for (int k = 0; k < ns; ++k) w->wdot[k] = 0.0;
+    for (int k = 0; k < ns; ++k) w->wdot[k] = 0.0, w->gross[k] = 0.0;
     for (int i = 0; i < nr; ++i) {
         double rf = w->kf[i], rr = w->kr[i];
         for (int e = m->net_off[i]; e < m->net_off[i + 1]; ++e) {
@@ -310,6 +311,8 @@ static void eval_rates(const orc_mech* m, int conp, double param, const double* 
         for (int e = m->net_off[i]; e < m->net_off[i + 1]; ++e) {
             int nu = m->net_nu[2 * e] - m->net_nu[2 * e + 1];
             w->wdot[m->net_spec[e]] = w->wdot[m->net_spec[e]] + nu * net;
+            double ci_ = m->rxn_thd[i] >= 0 ? fabs(w->pres_mod[m->rxn_thd[i]]) : 1.0;
+            w->gross[m->net_spec[e]] += fabs((double)nu) * (fabs(rf) + fabs(rr)) * ci_;
         }
     }
     /* molar rates, temperature and extra-variable rates (:709-1076) */
@@ -345,6 +348,14 @@ static void eval_rates(const orc_mech* m, int conp, double param, const double* 
         w->dphi[1] = P * w->dphi[0] / Tc;
         w->dphi[1] = w->dphi[1] + Tc * RU * dE;
     }
+    /* cancellation scale of each output: the same sums with absolute values */
+    double su = 0.0, sE = 0.0;
+    for (int k = 0; k < ns; ++k) su += fabs(w->h[k]) * w->gross[k];
+    for (int k = 0; k < last; ++k) sE += fabs(1.0 - m->mw_post[k]) * w->gross[k];
+    double sT = su / fabs(lower);
+    w->scale[0] = sT;
+    w->scale[1] = conp ? Vval * sT / Tc + Vval * sE * Tc * RU / P : P * sT / Tc + Tc * RU * sE;
+    for (int k = 0; k < last; ++k) w->scale[2 + k] = Vval * w->gross[k];
 }
 
 /* d ci / d x for a fall-off / chemically-activated reaction, given
@@ -771,7 +782,7 @@ static int ws_alloc(const orc_mech* m, ws* w)
     w->n_fall = nf;
     w->n_thd = nt;
     const int ns = m->ns, nr = m->nr, NN = ns + 1;
-    size_t tot = (size_t)ns * 9 + (size_t)nr * 4 + (size_t)(nf + 1) * 7 + (size_t)(nt + 1) * 2 + NN;
+    size_t tot = (size_t)ns * 10 + (size_t)nr * 4 + (size_t)(nf + 1) * 7 + (size_t)(nt + 1) * 2 + 2 * NN;
     double* p = (double*)calloc(tot, sizeof(double));
     if (!p) return -1;
     w->conc = p; p += ns;
@@ -781,6 +792,7 @@ static int ws_alloc(const orc_mech* m, ws* w)
     w->cp = p; p += ns;
     w->dcp = p; p += ns;
     w->db = p; p += ns;
+    w->gross = p; p += ns;
     p += 2 * ns;
     w->kf = p; p += nr;
     w->kr = p; p += nr;
@@ -795,7 +807,8 @@ static int ws_alloc(const orc_mech* m, ws* w)
     w->Xsri = p; p += nf + 1;
     w->thd_conc = p; p += nt + 1;
     w->pres_mod = p; p += nt + 1;
-    w->dphi = p;
+    w->dphi = p; p += NN;
+    w->scale = p;
     return 0;
 }
 
@@ -819,9 +832,12 @@ static int run(const orc_mech* m, long n, int conp, const double* param, const d
 #pragma omp for schedule(static)
 #endif
             for (long s = 0; s < n; ++s) {
-                if (jac) {
+                if (jac == 1) {
                     eval_jacobian(m, conp, param[s], phi + (size_t)s * NN, &w,
                                   out + (size_t)s * NN * NN);
+                } else if (jac == 2) {
+                    eval_rates(m, conp, param[s], phi + (size_t)s * NN, &w);
+                    memcpy(out + (size_t)s * NN, w.scale, sizeof(double) * NN);
                 } else {
                     eval_rates(m, conp, param[s], phi + (size_t)s * NN, &w);
                     memcpy(out + (size_t)s * NN, w.dphi, sizeof(double) * NN);
@@ -844,4 +860,10 @@ int orc_jacobian(const orc_mech* m, long n, int conp, const double* param, const
                  double* jac, int nthreads)
 {
     return run(m, n, conp, param, phi, jac, nthreads, 1);
+}
+
+int orc_rates_scale(const orc_mech* m, long n, int conp, const double* param, const double* phi,
+                    double* scale, int nthreads)
+{
+    return run(m, n, conp, param, phi, scale, nthreads, 2);
 }

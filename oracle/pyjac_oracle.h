@@ -70,6 +70,12 @@ int orc_species_rates(const orc_mech* m, long n, int conp, const double* param,
                       const double* phi, double* dphi, int nthreads);
 int orc_jacobian(const orc_mech* m, long n, int conp, const double* param,
                  const double* phi, double* jac, int nthreads);
+/* Cancellation scale of every dphi entry: the rate sums evaluated with
+ * absolute values (sum |nu| (|rop_f| + |rop_r|) |ci| per species, propagated
+ * through the T and extra-variable rates).  A parity metric, not a reference
+ * quantity. */
+int orc_rates_scale(const orc_mech* m, long n, int conp, const double* param,
+                    const double* phi, double* scale, int nthreads);
 
 #ifdef __cplusplus
 }

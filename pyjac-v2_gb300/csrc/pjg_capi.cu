@@ -1,0 +1,639 @@
+// C ABI of pyjac-v2_gb300 (declared in include/pyjac_gb300.h).
+//
+// Host responsibilities: validate and upload the mechanism tables, derive the
+// Jacobian slot tables for each output layout (dense/sparse x C/F), size the
+// per-state working arrays, chunk large problems, and launch the kernels of
+// pjg_eval.cu.  Mirrors the reference's generated Kernel class
+// (pyjac/kernel_utils/common/kernel.hpp.in:86-335, kernel.cpp.in:539-633):
+// problems are evaluated in chunks (the reference's max_per_run) with a
+// per-kernel-object device working buffer (the reference's rwk).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "../../include/pyjac_gb300.h"
+#include "pjg_eval.cuh"
+
+namespace {
+
+thread_local char g_err[512] = "";
+// kernel launches issued by this library, and optional per-launch timing of
+// the evaluation kernels (pjg_profile_begin / pjg_profile_end)
+std::atomic<int64_t> g_launches{0};
+std::atomic<bool> g_prof_on{false};
+std::mutex g_prof_mu;
+std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_prof_events;
+
+int fail(int code, const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CUDA_TRY(x)                                                                   \
+    do {                                                                              \
+        cudaError_t e_ = (x);                                                         \
+        if (e_ != cudaSuccess)                                                        \
+            return fail(PJG_ERR_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_));   \
+    } while (0)
+
+template <class T>
+int upload(const std::vector<T>& h, T** d)
+{
+    *d = nullptr;
+    size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
+    CUDA_TRY(cudaMalloc((void**)d, bytes));
+    if (!h.empty()) CUDA_TRY(cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+struct SlotTables {
+    int nslot = 0;
+    int *rxn_slot_off = nullptr, *rxn_slots = nullptr;
+    int *row_off = nullptr, *col_off = nullptr;
+    int2 *row_list = nullptr, *col_list = nullptr;
+    int *sp_slots = nullptr, *cj_slots = nullptr;
+    int s00 = 0, s01 = 0, s10 = 0, s11 = 0;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct pjg_mech {
+    int ns = 0, nr = 0, nn = 0, need_logP = 0, nnz = 0;
+    int device = 0;
+    PjgRxn* rxn = nullptr;
+    double* sp = nullptr;
+    int* thd_spec = nullptr;
+    double* thd_coef = nullptr;
+    double* aux = nullptr;
+    // host copies used to derive slot tables
+    std::vector<PjgRxn> h_rxn;
+    std::vector<int> h_thd_spec;
+    std::vector<int> crs_ptr, crs_ind, ccs_ptr, ccs_ind;
+    std::map<int, SlotTables> slots;  // key: (order == 'F') * 2 + sparse
+    std::mutex lock;
+    // working buffer shared by device-pointer calls on this mechanism
+    double* work = nullptr;
+    size_t work_bytes = 0;
+};
+
+struct pjg_kernel {
+    pjg_mech* mech = nullptr;
+    int kind = 0, conp = 1, jac_format = 0;
+    char order = 'C';
+    size_t problem_size = 0, work_size = 0;
+    double *d_param = nullptr, *d_phi = nullptr, *d_out = nullptr;
+    size_t out_per_state = 0;
+    cudaStream_t stream = nullptr;
+};
+
+namespace {
+
+int slot_of(const pjg_mech* m, bool F, bool sparse, int r, int c)
+{
+    const int NN = m->nn;
+    if (!sparse) return F ? r + NN * c : r * NN + c;
+    if (!F) {
+        for (int q = m->crs_ptr[r]; q < m->crs_ptr[r + 1]; ++q)
+            if (m->crs_ind[q] == c) return q;
+        return -1;
+    }
+    for (int q = m->ccs_ptr[c]; q < m->ccs_ptr[c + 1]; ++q)
+        if (m->ccs_ind[q] == r) return q;
+    return -1;
+}
+
+int build_slots(pjg_mech* m, bool F, bool sparse, SlotTables** out)
+{
+    const int key = (F ? 2 : 0) + (sparse ? 1 : 0);
+    std::lock_guard<std::mutex> g(m->lock);
+    auto it = m->slots.find(key);
+    if (it != m->slots.end()) {
+        *out = &it->second;
+        return 0;
+    }
+    const int ns = m->ns, last = ns - 1, NN = m->nn;
+    SlotTables t;
+    t.nslot = sparse ? m->nnz : NN * NN;
+    std::vector<int> off(m->nr + 1, 0), list;
+    for (int i = 0; i < m->nr; ++i) {
+        const PjgRxn& R = m->h_rxn[i];
+        const int nsp = R.nspec;
+        off[i] = (int)list.size();
+        for (int a = 0; a < nsp; ++a)
+            for (int b = 0; b < nsp; ++b) {
+                const int k = ent_spec(R.ent[a]), j = ent_spec(R.ent[b]);
+                list.push_back(k == last || j == last ? -1 : slot_of(m, F, sparse, 2 + k, 2 + j));
+            }
+        for (int a = 0; a < nsp; ++a) {
+            const int k = ent_spec(R.ent[a]);
+            list.push_back(k == last ? -1 : slot_of(m, F, sparse, 2 + k, 0));
+            list.push_back(k == last ? -1 : slot_of(m, F, sparse, 2 + k, 1));
+        }
+        for (int l = 0; l < R.thd_cnt; ++l) {
+            const int j = m->h_thd_spec[R.thd_off + l];
+            for (int a = 0; a < nsp; ++a) {
+                const int k = ent_spec(R.ent[a]);
+                list.push_back(k == last || j == last ? -1 : slot_of(m, F, sparse, 2 + k, 2 + j));
+            }
+        }
+    }
+    off[m->nr] = (int)list.size();
+    std::vector<int> row_off(ns, 0), col_off(ns, 0), sp_slots(2 * std::max(last, 1), -1),
+        cj_slots(2 * std::max(last, 1), -1);
+    std::vector<int2> row_list, col_list;
+    for (int k = 0; k < last; ++k) {
+        row_off[k] = (int)row_list.size();
+        for (int j = 0; j < last; ++j) {
+            const int sl = slot_of(m, F, sparse, 2 + k, 2 + j);
+            if (sl >= 0) row_list.push_back(make_int2(j, sl));
+        }
+        sp_slots[2 * k] = slot_of(m, F, sparse, 2 + k, 0);
+        sp_slots[2 * k + 1] = slot_of(m, F, sparse, 2 + k, 1);
+    }
+    row_off[last] = (int)row_list.size();
+    for (int j = 0; j < last; ++j) {
+        col_off[j] = (int)col_list.size();
+        for (int k = 0; k < last; ++k) {
+            const int sl = slot_of(m, F, sparse, 2 + k, 2 + j);
+            if (sl >= 0) col_list.push_back(make_int2(k, sl));
+        }
+        cj_slots[2 * j] = slot_of(m, F, sparse, 0, 2 + j);
+        cj_slots[2 * j + 1] = slot_of(m, F, sparse, 1, 2 + j);
+        if (cj_slots[2 * j] < 0 || cj_slots[2 * j + 1] < 0)
+            return fail(PJG_ERR_TABLES, "Jacobian pattern lacks entries of rows T/E");
+    }
+    col_off[last] = (int)col_list.size();
+    t.s00 = slot_of(m, F, sparse, 0, 0);
+    t.s01 = slot_of(m, F, sparse, 0, 1);
+    t.s10 = slot_of(m, F, sparse, 1, 0);
+    t.s11 = slot_of(m, F, sparse, 1, 1);
+    if (t.s00 < 0 || t.s01 < 0 || t.s10 < 0 || t.s11 < 0)
+        return fail(PJG_ERR_TABLES, "Jacobian pattern lacks the T/E block");
+    int rc;
+    if ((rc = upload(off, &t.rxn_slot_off)) || (rc = upload(list, &t.rxn_slots)) ||
+        (rc = upload(row_off, &t.row_off)) || (rc = upload(row_list, &t.row_list)) ||
+        (rc = upload(col_off, &t.col_off)) || (rc = upload(col_list, &t.col_list)) ||
+        (rc = upload(sp_slots, &t.sp_slots)) || (rc = upload(cj_slots, &t.cj_slots)))
+        return rc;
+    t.bytes = (off.size() + list.size() + row_off.size() + col_off.size() + sp_slots.size() +
+               cj_slots.size()) * sizeof(int) + (row_list.size() + col_list.size()) * sizeof(int2);
+    auto res = m->slots.emplace(key, t);
+    *out = &res.first->second;
+    return 0;
+}
+
+// per-state bytes of working arrays for one evaluation
+size_t state_bytes(const pjg_mech* m, int kind, bool c_order_jac, int nslot)
+{
+    size_t arrs = kind == PJG_JACOBIAN ? ARR_N_JAC : ARR_N_RATES;
+    size_t b = arrs * m->ns * sizeof(double);
+    if (kind == PJG_JACOBIAN && c_order_jac) b += (size_t)nslot * sizeof(double);
+    return b;
+}
+
+bool rates_fit_smem(const pjg_mech* m)
+{
+    return (size_t)ARR_N_RATES * m->ns * PJG_BLOCK * sizeof(double) <= 200 * 1024;
+}
+
+constexpr size_t kWorkBudget = size_t(1) << 30;  // bytes of working buffer per call
+
+int64_t chunk_states(size_t per_state, int64_t n)
+{
+    if (per_state == 0) return n;
+    int64_t c = (int64_t)(kWorkBudget / per_state);
+    c = std::max<int64_t>(PJG_BLOCK, c / PJG_BLOCK * PJG_BLOCK);
+    return std::min<int64_t>(c, n);
+}
+
+int ensure_work(pjg_mech* m, size_t bytes)
+{
+    if (bytes <= m->work_bytes) return 0;
+    if (m->work) cudaFree(m->work);
+    m->work = nullptr;
+    m->work_bytes = 0;
+    CUDA_TRY(cudaMalloc((void**)&m->work, bytes));
+    m->work_bytes = bytes;
+    return 0;
+}
+
+void fill_common(const pjg_mech* m, EvalArgs& a)
+{
+    memset(&a, 0, sizeof(a));
+    a.rxn = m->rxn;
+    a.sp = m->sp;
+    a.thd_spec = m->thd_spec;
+    a.thd_coef = m->thd_coef;
+    a.aux = m->aux;
+    a.ns = m->ns;
+    a.nr = m->nr;
+    a.need_logP = m->need_logP;
+}
+
+int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_format,
+             const double* param, const double* phi, double* out, cudaStream_t st)
+{
+    if (!m) return fail(PJG_ERR_ARG, "null mechanism");
+    if (n < 0) return fail(PJG_ERR_ARG, "negative problem size");
+    if (order != 'C' && order != 'F') return fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
+    if (jac_format != PJG_JAC_FULL && jac_format != PJG_JAC_SPARSE)
+        return fail(PJG_ERR_ARG, "jac_format must be 0 (full) or 1 (sparse)");
+    if (n == 0) return 0;
+    if (!param || !phi || !out) return fail(PJG_ERR_ARG, "null array");
+    const bool F = order == 'F';
+    const int NN = m->nn;
+    SlotTables* t = nullptr;
+    if (kind == PJG_JACOBIAN) {
+        int rc = build_slots(m, F, jac_format == PJG_JAC_SPARSE, &t);
+        if (rc) return rc;
+    }
+    const bool smem = kind == PJG_SPECIES_RATES && rates_fit_smem(m);
+    size_t per_state = smem ? 0 : state_bytes(m, kind, !F, t ? t->nslot : 0);
+    if (kind == PJG_JACOBIAN && !F) per_state = state_bytes(m, kind, true, t->nslot);
+    const int64_t ch = chunk_states(per_state, n);
+    if (per_state) {
+        int rc = ensure_work(m, per_state * (size_t)ch);
+        if (rc) return rc;
+    }
+    for (int64_t off = 0; off < n; off += ch) {
+        const int64_t cnt = std::min<int64_t>(ch, n - off);
+        EvalArgs a;
+        fill_common(m, a);
+        a.n = cnt;
+        a.conp = conp;
+        a.param = param + off;
+        if (F) {
+            a.phi = phi + off;
+            a.phi_ss = 1;
+            a.phi_sj = n;
+        } else {
+            a.phi = phi + off * NN;
+            a.phi_ss = NN;
+            a.phi_sj = 1;
+        }
+        a.use_smem = smem;
+        a.scratch = m->work;
+        a.sc_ld = ch;
+        size_t smem_bytes = smem ? (size_t)ARR_N_RATES * m->ns * PJG_BLOCK * sizeof(double) : 0;
+        if (kind == PJG_SPECIES_RATES) {
+            a.dphi = F ? out + off : out + off * NN;
+            a.dphi_ss = a.phi_ss;
+            a.dphi_sj = a.phi_sj;
+        } else {
+            a.nslot = t->nslot;
+            if (F) {
+                a.acc = out + off;
+                a.acc_ld = n;
+            } else {
+                a.acc = m->work + (size_t)ARR_N_JAC * m->ns * ch;
+                a.acc_ld = ch;
+            }
+            a.rxn_slot_off = t->rxn_slot_off;
+            a.rxn_slots = t->rxn_slots;
+            a.row_off = t->row_off;
+            a.row_list = t->row_list;
+            a.col_off = t->col_off;
+            a.col_list = t->col_list;
+            a.sp_slots = t->sp_slots;
+            a.cj_slots = t->cj_slots;
+            a.s00 = t->s00;
+            a.s01 = t->s01;
+            a.s10 = t->s10;
+            a.s11 = t->s11;
+        }
+        int rc = 0;
+        if (kind == PJG_JACOBIAN) {
+            rc = pjg_launch_zero(a.acc, a.acc_ld, cnt, a.nslot, st);
+            if (rc) return fail(PJG_ERR_CUDA, "zero launch failed");
+            g_launches.fetch_add(1);
+        }
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        const bool prof = g_prof_on.load();
+        if (prof) {
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            cudaEventRecord(e0, st);
+        }
+        rc = pjg_launch_eval(a, kind, st, smem_bytes);
+        if (rc) return fail(PJG_ERR_CUDA, "kernel launch failed: %s",
+                            cudaGetErrorString(cudaGetLastError()));
+        g_launches.fetch_add(1);
+        if (prof) {
+            cudaEventRecord(e1, st);
+            std::lock_guard<std::mutex> g(g_prof_mu);
+            g_prof_events.emplace_back(e0, e1);
+        }
+        if (kind == PJG_JACOBIAN && !F) {
+            rc = pjg_launch_transpose(a.acc, a.acc_ld, cnt, t->nslot, out + off * (int64_t)t->nslot,
+                                      st);
+            if (rc) return fail(PJG_ERR_CUDA, "transpose launch failed");
+            g_launches.fetch_add(1);
+        }
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pjg_last_error(char* buf, size_t len)
+{
+    if (!buf || len == 0) return PJG_ERR_ARG;
+    snprintf(buf, len, "%s", g_err);
+    return 0;
+}
+
+int pjg_fp64_peak(double* tflops)
+{
+    if (!tflops) return fail(PJG_ERR_ARG, "null argument");
+    int dev = 0, sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    double* out = nullptr;
+    CUDA_TRY(cudaMalloc((void**)&out, sizeof(double) * 64 * sms));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = 8 * sms, threads = 256, iters = 4096;
+    int rc = pjg_fp64_probe(blocks, threads, 64, out, nullptr);  // warm-up
+    cudaEventRecord(e0, nullptr);
+    rc |= pjg_fp64_probe(blocks, threads, iters, out, nullptr);
+    cudaEventRecord(e1, nullptr);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (rc) return fail(PJG_ERR_CUDA, "fp64 probe launch failed");
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+    return 0;
+}
+
+int pjg_launch_count(int64_t* count)
+{
+    if (!count) return fail(PJG_ERR_ARG, "null argument");
+    *count = g_launches.load();
+    return 0;
+}
+
+int pjg_profile_begin(void)
+{
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    for (auto& e : g_prof_events) {
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    g_prof_events.clear();
+    g_prof_on.store(true);
+    return 0;
+}
+
+int pjg_profile_end(int64_t* launches, double* total_ms)
+{
+    g_prof_on.store(false);
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    double tot = 0.0;
+    int rc = 0;
+    for (auto& e : g_prof_events) {
+        float ms = 0.0f;
+        if (cudaEventSynchronize(e.second) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e.first, e.second) != cudaSuccess)
+            rc = fail(PJG_ERR_CUDA, "profiling event query failed");
+        tot += ms;
+        cudaEventDestroy(e.first);
+        cudaEventDestroy(e.second);
+    }
+    if (launches) *launches = (int64_t)g_prof_events.size();
+    if (total_ms) *total_ms = tot;
+    g_prof_events.clear();
+    return rc;
+}
+
+int pjg_mech_create(const pjg_tables* tb, pjg_mech** out)
+{
+    if (!tb || !out) return fail(PJG_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (tb->ns < 2 || tb->nr < 0 || !tb->species || (tb->nr > 0 && !tb->rxn))
+        return fail(PJG_ERR_TABLES, "invalid species/reaction counts");
+    const int NN = tb->ns + 1;
+    if (tb->nnz <= 0 || !tb->crs_row_ptr || !tb->crs_col_ind || !tb->ccs_col_ptr || !tb->ccs_row_ind)
+        return fail(PJG_ERR_TABLES, "missing Jacobian pattern");
+    pjg_mech* m = new pjg_mech();
+    m->ns = tb->ns;
+    m->nr = tb->nr;
+    m->nn = NN;
+    m->need_logP = tb->flags & 1;
+    m->nnz = tb->nnz;
+    cudaGetDevice(&m->device);
+    const PjgRxn* r = (const PjgRxn*)tb->rxn;
+    m->h_rxn.assign(r, r + tb->nr);
+    m->h_thd_spec.assign(tb->thd_spec, tb->thd_spec + std::max(tb->n_thd, 0));
+    for (const PjgRxn& R : m->h_rxn) {
+        if (R.nspec < 1 || R.nspec > PJG_MAXSP || R.thd_off < 0 || R.thd_cnt < 0 ||
+            R.thd_off + R.thd_cnt > tb->n_thd) {
+            delete m;
+            return fail(PJG_ERR_TABLES, "reaction record out of range");
+        }
+        for (int e = 0; e < R.nspec; ++e)
+            if (ent_spec(R.ent[e]) >= tb->ns) {
+                delete m;
+                return fail(PJG_ERR_TABLES, "species index out of range");
+            }
+        if (RX_FORM(R.flags) >= FORM_PLOG && (R.aux < 0 || R.aux >= tb->n_aux)) {
+            delete m;
+            return fail(PJG_ERR_TABLES, "PLOG/Chebyshev block out of range");
+        }
+    }
+    for (int l = 0; l < tb->n_thd; ++l)
+        if (tb->thd_spec[l] < 0 || tb->thd_spec[l] >= tb->ns) {
+            delete m;
+            return fail(PJG_ERR_TABLES, "third-body species out of range");
+        }
+    m->crs_ptr.assign(tb->crs_row_ptr, tb->crs_row_ptr + NN + 1);
+    m->crs_ind.assign(tb->crs_col_ind, tb->crs_col_ind + tb->nnz);
+    m->ccs_ptr.assign(tb->ccs_col_ptr, tb->ccs_col_ptr + NN + 1);
+    m->ccs_ind.assign(tb->ccs_row_ind, tb->ccs_row_ind + tb->nnz);
+    if (m->crs_ptr[NN] != tb->nnz || m->ccs_ptr[NN] != tb->nnz) {
+        delete m;
+        return fail(PJG_ERR_TABLES, "pattern pointers inconsistent with nnz");
+    }
+    std::vector<PjgRxn> rx(m->h_rxn);
+    std::vector<double> sp(tb->species, tb->species + (size_t)tb->ns * PJG_SP_DOUBLES);
+    std::vector<double> coef(tb->thd_coef, tb->thd_coef + std::max(tb->n_thd, 0));
+    std::vector<double> aux(tb->aux ? tb->aux : (const double*)nullptr,
+                            tb->aux ? tb->aux + std::max(tb->n_aux, 0) : (const double*)nullptr);
+    int rc;
+    if ((rc = upload(rx, &m->rxn)) || (rc = upload(sp, &m->sp)) ||
+        (rc = upload(m->h_thd_spec, &m->thd_spec)) || (rc = upload(coef, &m->thd_coef)) ||
+        (rc = upload(aux, &m->aux))) {
+        pjg_mech_destroy(m);
+        return rc;
+    }
+    *out = m;
+    return 0;
+}
+
+int pjg_mech_destroy(pjg_mech* m)
+{
+    if (!m) return 0;
+    cudaFree(m->rxn);
+    cudaFree(m->sp);
+    cudaFree(m->thd_spec);
+    cudaFree(m->thd_coef);
+    cudaFree(m->aux);
+    cudaFree(m->work);
+    for (auto& kv : m->slots) {
+        SlotTables& t = kv.second;
+        cudaFree(t.rxn_slot_off);
+        cudaFree(t.rxn_slots);
+        cudaFree(t.row_off);
+        cudaFree(t.row_list);
+        cudaFree(t.col_off);
+        cudaFree(t.col_list);
+        cudaFree(t.sp_slots);
+        cudaFree(t.cj_slots);
+    }
+    delete m;
+    return 0;
+}
+
+int pjg_mech_info(const pjg_mech* m, int32_t* ns, int32_t* nr, int32_t* nnz)
+{
+    if (!m) return fail(PJG_ERR_ARG, "null mechanism");
+    if (ns) *ns = m->ns;
+    if (nr) *nr = m->nr;
+    if (nnz) *nnz = m->nnz;
+    return 0;
+}
+
+int pjg_jacobian_indices(const pjg_mech* m, char order, int32_t* ptr, int32_t* ind, int32_t* nnz)
+{
+    if (!m) return fail(PJG_ERR_ARG, "null mechanism");
+    if (order != 'C' && order != 'F') return fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
+    const std::vector<int>& p = order == 'C' ? m->crs_ptr : m->ccs_ptr;
+    const std::vector<int>& q = order == 'C' ? m->crs_ind : m->ccs_ind;
+    if (nnz) *nnz = m->nnz;
+    if (ptr) memcpy(ptr, p.data(), p.size() * sizeof(int32_t));
+    if (ind) memcpy(ind, q.data(), q.size() * sizeof(int32_t));
+    return 0;
+}
+
+int pjg_species_rates(pjg_mech* m, int64_t n, char order, int conp, const double* param,
+                      const double* phi, double* dphi, void* stream)
+{
+    return run_eval(m, PJG_SPECIES_RATES, n, order, conp, 0, param, phi, dphi, (cudaStream_t)stream);
+}
+
+int pjg_jacobian(pjg_mech* m, int64_t n, char order, int conp, int jac_format, const double* param,
+                 const double* phi, double* jac, void* stream)
+{
+    return run_eval(m, PJG_JACOBIAN, n, order, conp, jac_format, param, phi, jac,
+                    (cudaStream_t)stream);
+}
+
+int pjg_vjp(pjg_mech* m, int64_t n, char order, int conp, const double* param, const double* phi,
+            const double* v, double* out, void* stream)
+{
+    (void)m; (void)n; (void)order; (void)conp; (void)param; (void)phi; (void)v; (void)out;
+    (void)stream;
+    return fail(PJG_ERR_UNSUPPORTED, "pjg_vjp not available in this build");
+}
+
+int pjg_kernel_create(pjg_mech* m, int kind, size_t problem_size, size_t work_size, char order,
+                      int conp, int jac_format, pjg_kernel** out)
+{
+    if (!m || !out) return fail(PJG_ERR_ARG, "null argument");
+    if (kind != PJG_SPECIES_RATES && kind != PJG_JACOBIAN) return fail(PJG_ERR_ARG, "bad kind");
+    if (order != 'C' && order != 'F') return fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
+    if (jac_format != PJG_JAC_FULL && jac_format != PJG_JAC_SPARSE)
+        return fail(PJG_ERR_ARG, "bad jac_format");
+    pjg_kernel* k = new pjg_kernel();
+    k->mech = m;
+    k->kind = kind;
+    k->order = order;
+    k->conp = conp;
+    k->jac_format = jac_format;
+    k->out_per_state = kind == PJG_SPECIES_RATES ? m->nn
+                       : (jac_format == PJG_JAC_SPARSE ? (size_t)m->nnz : (size_t)m->nn * m->nn);
+    if (cudaStreamCreateWithFlags(&k->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete k;
+        return fail(PJG_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    int rc = pjg_kernel_resize(k, problem_size, work_size);
+    if (rc) {
+        pjg_kernel_destroy(k);
+        return rc;
+    }
+    *out = k;
+    return 0;
+}
+
+int pjg_kernel_resize(pjg_kernel* k, size_t problem_size, size_t work_size)
+{
+    if (!k) return fail(PJG_ERR_ARG, "null kernel");
+    k->work_size = work_size;
+    if (problem_size == k->problem_size && k->d_phi) return 0;
+    cudaFree(k->d_param);
+    cudaFree(k->d_phi);
+    cudaFree(k->d_out);
+    k->d_param = k->d_phi = k->d_out = nullptr;
+    k->problem_size = problem_size;
+    if (problem_size == 0) return 0;
+    const size_t nn = k->mech->nn;
+    CUDA_TRY(cudaMalloc((void**)&k->d_param, problem_size * sizeof(double)));
+    CUDA_TRY(cudaMalloc((void**)&k->d_phi, problem_size * nn * sizeof(double)));
+    CUDA_TRY(cudaMalloc((void**)&k->d_out, problem_size * k->out_per_state * sizeof(double)));
+    return 0;
+}
+
+int pjg_kernel_call(pjg_kernel* k, const double* param, const double* phi, double* out)
+{
+    if (!k) return fail(PJG_ERR_ARG, "null kernel");
+    const size_t n = k->problem_size, nn = k->mech->nn;
+    if (n == 0) return 0;
+    if (!param || !phi || !out) return fail(PJG_ERR_ARG, "null array");
+    CUDA_TRY(cudaMemcpyAsync(k->d_param, param, n * sizeof(double), cudaMemcpyHostToDevice, k->stream));
+    CUDA_TRY(cudaMemcpyAsync(k->d_phi, phi, n * nn * sizeof(double), cudaMemcpyHostToDevice, k->stream));
+    int rc = run_eval(k->mech, k->kind, (int64_t)n, k->order, k->conp, k->jac_format, k->d_param,
+                      k->d_phi, k->d_out, k->stream);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(out, k->d_out, n * k->out_per_state * sizeof(double),
+                             cudaMemcpyDeviceToHost, k->stream));
+    CUDA_TRY(cudaStreamSynchronize(k->stream));
+    return 0;
+}
+
+int pjg_kernel_required_memory(const pjg_kernel* k, size_t* bytes)
+{
+    if (!k || !bytes) return fail(PJG_ERR_ARG, "null argument");
+    *bytes = k->problem_size * (1 + k->mech->nn + k->out_per_state) * sizeof(double) +
+             k->mech->work_bytes;
+    return 0;
+}
+
+int pjg_kernel_destroy(pjg_kernel* k)
+{
+    if (!k) return 0;
+    cudaFree(k->d_param);
+    cudaFree(k->d_phi);
+    cudaFree(k->d_out);
+    if (k->stream) cudaStreamDestroy(k->stream);
+    delete k;
+    return 0;
+}
+
+}  // extern "C"

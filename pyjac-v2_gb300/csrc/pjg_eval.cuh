@@ -1,0 +1,69 @@
+// Kernel argument block and per-state array layout shared by the evaluation
+// kernels (pjg_eval.cu) and their host launcher (pjg_capi.cu).
+#pragma once
+#include <cstdint>
+#include "pjg_tables.cuh"
+
+#define PJG_BLOCK 128
+
+// per-state arrays (each ns doubles)
+enum {
+    ARR_CONC = 0,  // concentrations c_k
+    ARR_B,         // Gibbs function b_k (Kc)
+    ARR_WDOT,      // net molar production rates
+    ARR_N_RATES,
+    ARR_DB = ARR_N_RATES,  // d b_k / dT
+    ARR_NSROW,     // per-row sum of bath-gas terms, subtracted from every species column
+    ARR_HW,        // h_k - h_ns W_k / W_ns (row-0 weights)
+    ARR_CP,        // specific heats
+    ARR_DCP,       // d cp_k / dT
+    ARR_H,         // specific enthalpies (energies at constant volume)
+    ARR_N_JAC
+};
+
+struct EvalArgs {
+    // mechanism
+    const PjgRxn* rxn;
+    const double* sp;
+    const int* thd_spec;
+    const double* thd_coef;
+    const double* aux;
+    int ns, nr;
+    int need_logP;
+    // states
+    int64_t n;  // states in this launch
+    int conp;
+    const double* param;
+    const double* phi;
+    int64_t phi_ss, phi_sj;  // element (s, j) at phi[s * phi_ss + j * phi_sj]
+    double* dphi;            // optional
+    int64_t dphi_ss, dphi_sj;
+    // per-state arrays: global scratch (arr a, species k, state s at
+    // scratch[(a * ns + k) * sc_ld + s]) unless use_smem
+    double* scratch;
+    int64_t sc_ld;
+    int use_smem;
+    // Jacobian accumulator: acc[slot * acc_ld + s]
+    double* acc;
+    int64_t acc_ld;
+    int nslot;
+    const int* rxn_slot_off;  // nr + 1
+    const int* rxn_slots;
+    const int* row_off;       // ns (rows of species 0..ns-2)
+    const int2* row_list;     // (species column j, slot)
+    const int* col_off;       // ns
+    const int2* col_list;     // (species row k, slot)
+    const int* sp_slots;      // 2 per species row: slot(k, T), slot(k, E)
+    const int* cj_slots;      // 2 per species column: slot(T, j), slot(E, j)
+    int s00, s01, s10, s11;
+    // vector-Jacobian product
+    const double* v;          // v[s * phi_ss + j * phi_sj]
+    double* vjp;              // same layout
+};
+
+// host launchers (pjg_eval.cu)
+int pjg_launch_eval(const EvalArgs& a, int kind, void* stream, size_t smem_bytes);
+int pjg_launch_zero(double* acc, int64_t ld, int64_t n, int nslot, void* stream);
+int pjg_fp64_probe(int blocks, int threads, int iters, double* out, void* stream);
+int pjg_launch_transpose(const double* src, int64_t ld, int64_t n, int nslot, double* dst,
+                         void* stream);

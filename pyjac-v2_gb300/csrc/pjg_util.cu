@@ -1,0 +1,71 @@
+// Auxiliary kernels: accumulator zeroing, state-innermost -> 'C' transpose,
+// and the FP64 throughput probe used as the FP64 roofline denominator.
+#include <cuda_runtime.h>
+#include "pjg_eval.cuh"
+
+namespace {
+
+__global__ void zero_acc(double* acc, int64_t ld, int64_t n, int nslot)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    for (int q = 0; q < nslot; ++q) acc[(int64_t)q * ld + s] = 0.0;
+}
+
+// dst[s * nslot + q] = src[q * ld + s] through 32 x 32 shared-memory tiles.
+__global__ void transpose_kernel(const double* __restrict__ src, int64_t ld, int64_t n, int nslot,
+                                 double* __restrict__ dst)
+{
+    __shared__ double tile[32][33];
+    const int64_t s0 = (int64_t)blockIdx.x * 32;
+    const int q0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int q = q0 + r;
+        const int64_t s = s0 + threadIdx.x;
+        if (q < nslot && s < n) tile[r][threadIdx.x] = src[(int64_t)q * ld + s];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int64_t s = s0 + r;
+        const int q = q0 + threadIdx.x;
+        if (q < nslot && s < n) dst[s * nslot + q] = tile[threadIdx.x][r];
+    }
+}
+
+// FP64 FMA throughput probe: 8 independent dependency chains per thread.
+__global__ void dfma_probe(double* out, int iters, double a, double b)
+{
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
+           x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 1.2345) out[blockIdx.x] = s;  // keeps the chains live, never true in practice
+}
+
+}  // namespace
+
+int pjg_fp64_probe(int blocks, int threads, int iters, double* out, void* stream)
+{
+    dfma_probe<<<blocks, threads, 0, (cudaStream_t)stream>>>(out, iters, 0.999999, 1e-7);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int pjg_launch_zero(double* acc, int64_t ld, int64_t n, int nslot, void* stream)
+{
+    if (n <= 0) return 0;
+    const unsigned grid = (unsigned)((n + PJG_BLOCK - 1) / PJG_BLOCK);
+    zero_acc<<<grid, PJG_BLOCK, 0, (cudaStream_t)stream>>>(acc, ld, n, nslot);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int pjg_launch_transpose(const double* src, int64_t ld, int64_t n, int nslot, double* dst,
+                         void* stream)
+{
+    if (n <= 0 || nslot <= 0) return 0;
+    dim3 grid((unsigned)((n + 31) / 32), (unsigned)((nslot + 31) / 32));
+    transpose_kernel<<<grid, dim3(32, 8), 0, (cudaStream_t)stream>>>(src, ld, n, nslot, dst);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}

@@ -80,6 +80,17 @@ def _is_int(v):
     return float(v).is_integer()
 
 
+def _stack(arrays):
+    """np.array of equally shaped arrays; an object array when they are ragged."""
+    try:
+        return np.array(arrays)
+    except ValueError:
+        out = np.empty(len(arrays), dtype=object)
+        for i, a in enumerate(arrays):
+            out[i] = a
+        return out
+
+
 def _specialize(rates, rate_spec, fall=False):
     """Per-reaction Arrhenius parameters and rate type (rate_subs.py:219-266)."""
     n = len(rates)
@@ -271,7 +282,7 @@ def assign_rates(reacs, specs, rate_spec="hybrid"):
                      "params": plog_params, "max_P": maxP,
                      "post_process": {"params": pp_plog}},
             "cheb": {"map": cheb_map, "num": n_cheb, "num_P": cheb_nP, "num_T": cheb_nT,
-                     "params": [np.array(r.cheb_par, dtype=np.float64) for r in cheb],
+                     "params": _stack([np.array(r.cheb_par, dtype=np.float64) for r in cheb]),
                      "Tlim": cheb_tlim, "Plim": cheb_plim,
                      "post_process": {"params": pp_cheb, "Plim": pp_cheb_plim,
                                       "Tlim": pp_cheb_tlim}},

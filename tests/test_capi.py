@@ -1,0 +1,78 @@
+"""C ABI checks that need no GPU: the library builds, loads, exports every
+function include/pyjac_gb300.h declares, and rejects bad arguments with an
+error status (never an abort) before touching the device."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_mech, pkg
+
+
+def declared_functions():
+    with open(os.path.join(ROOT, "include", "pyjac_gb300.h")) as fh:
+        text = fh.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\bint\s+(pjg_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    pkg("build").build()
+    return pkg("_lib").load()
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+    bound = {s[0] for s in pkg("_lib").SIGNATURES}
+    assert set(names) <= bound
+
+
+def test_bad_arguments_return_status(lib):
+    L = pkg("_lib")
+    assert lib.pjg_mech_create(None, None) == -1
+    assert "null" in L.last_error()
+    t = L.PjgTables()
+    t.ns = 1
+    h = ctypes.c_void_p()
+    assert lib.pjg_mech_create(ctypes.byref(t), ctypes.byref(h)) == -3
+    assert lib.pjg_species_rates(None, 10, b"C", 1, None, None, None, None) == -1
+    assert lib.pjg_jacobian(None, 10, b"C", 1, 0, None, None, None, None) == -1
+    assert lib.pjg_kernel_call(None, None, None, None) == -1
+    assert lib.pjg_jacobian_indices(None, b"C", None, None, None) == -1
+    buf = ctypes.create_string_buffer(4)
+    assert lib.pjg_last_error(buf, 4) == 0 and len(buf.value) <= 3
+
+
+def test_packed_tables_layout():
+    pack = pkg("pack")
+    mech = load_mech("gri30")
+    pt = pack.PackedTables(mech)
+    assert pt.rxn.dtype.itemsize == 192 and len(pt.rxn) == 325
+    assert pt.species.shape == (53, 48)
+    flags = pt.rxn["flags"]
+    assert ((flags & 7) <= 2).all()                      # no PLOG / Chebyshev in GRI
+    assert int(((flags >> 4) & 3 != 0).sum()) == 41      # third-body + fall-off reactions
+    assert int(((flags >> 6) & 3 == 2).sum()) == 26      # Troe
+    assert int((flags & pack.RX_REV != 0).sum()) == 309  # reversible
+    assert pt.nnz == 1984
+    mt = pkg("mech")
+    tm = load_mech("testmech")
+    ft = pack.PackedTables(tm).rxn["flags"]
+    assert (ft & 7 == 3).sum() == tm.val["plog"]["num"]
+    assert (ft & 7 == 4).sum() == tm.val["cheb"]["num"]
+    assert mt is not None
+
+
+def test_product_path_has_no_cpu_fallback(monkeypatch, tmp_path):
+    """Without the CUDA library the API raises instead of computing on the CPU."""
+    L = pkg("_lib")
+    monkeypatch.setattr(L, "_lib", None)
+    monkeypatch.setattr(L, "library_path", lambda: str(tmp_path / "missing.so"))
+    with pytest.raises(RuntimeError):
+        pkg("api").Evaluator(load_mech("h2o2"))

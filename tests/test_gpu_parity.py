@@ -1,0 +1,148 @@
+"""GPU parity: the CUDA kernels through the C ABI against the CPU oracle.
+
+Tolerances (the spec bars):
+* species rates: |gpu - ref| <= 1e-10 * (|ref| + s), s = cancellation scale of
+  the entry (the same rate sums with absolute values, oracle.rates_scale);
+* Jacobian: |gpu - ref| <= 1e-8 * max_col |ref[row]| (row-relative);
+* sparse values equal the dense values at the pattern's (row, col).
+"""
+import numpy as np
+import pytest
+
+from conftest import (bath_rich_states, load_mech, oracle_mod, pkg, rel_err, row_rel_err)
+
+pytestmark = pytest.mark.gpu
+
+RTOL_RATES = 1e-10
+RTOL_JAC = 1e-8
+MECHS = ["h2o2", "gri30", "testmech", "synthetic_small"]
+
+_ev = {}
+
+
+def evaluator(name):
+    if name not in _ev:
+        _ev[name] = pkg("api").Evaluator(load_mech(name))
+    return _ev[name]
+
+
+def states(name, n, seed, conp):
+    mech = load_mech(name)
+    if name == "gri30":
+        return pkg("states").draw_states(mech.n_species, n, seed=seed, x_floor=1e-12, conp=conp)
+    if name == "h2o2":
+        return pkg("states").draw_states(mech.n_species, n, seed=seed, conp=conp)
+    return bath_rich_states(mech, n, seed, conp)
+
+
+def to_dev(a, device):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device)
+
+
+def rates_ok(d, ref, scale):
+    den = np.abs(ref) + scale
+    diff = np.abs(d - ref)
+    err = np.where(den > 0, diff / np.where(den > 0, den, 1.0), np.where(diff > 0, np.inf, 0.0))
+    return float(err.max())
+
+
+@pytest.mark.parametrize("name", MECHS)
+@pytest.mark.parametrize("conp", [True, False])
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_species_rates(cuda_device, name, conp, order):
+    mech = load_mech(name)
+    n = 300  # not a multiple of the block size: exercises the ragged tail
+    P, phi = states(name, n, 11, conp)
+    o = oracle_mod().Oracle(mech)
+    ref = o.species_rates(P, phi, conp=conp)
+    scale = o.rates_scale(P, phi, conp=conp)
+    ev = evaluator(name)
+    x = phi if order == "C" else phi.T
+    d = ev.species_rates(to_dev(P, cuda_device), to_dev(x, cuda_device), order=order,
+                         conp=conp).cpu().numpy()
+    if order == "F":
+        d = d.T
+    assert np.isfinite(d).all()
+    assert rates_ok(d, ref, scale) < RTOL_RATES
+
+
+def _dense_from(out, order, fmt, mech, dm, n):
+    NN = mech.nn
+    if fmt == "full":
+        if order == "C":
+            return out.reshape(n, NN, NN)
+        # F: jac[i + N*row + N*NN*col]
+        return out.reshape(NN, NN, n).transpose(2, 1, 0)
+    ptr, ind = dm.jacobian_indices(order)
+    J = np.zeros((n, NN, NN))
+    vals = out.reshape(n, -1) if order == "C" else out.reshape(-1, n).T
+    for a in range(NN):
+        for p in range(ptr[a], ptr[a + 1]):
+            if order == "C":
+                J[:, a, ind[p]] = vals[:, p]
+            else:
+                J[:, ind[p], a] = vals[:, p]
+    return J
+
+
+@pytest.mark.parametrize("name", MECHS)
+@pytest.mark.parametrize("conp", [True, False])
+@pytest.mark.parametrize("order", ["C", "F"])
+@pytest.mark.parametrize("fmt", ["full", "sparse"])
+def test_jacobian(cuda_device, name, conp, order, fmt):
+    mech = load_mech(name)
+    n = 200
+    P, phi = states(name, n, 12, conp)
+    o = oracle_mod().Oracle(mech)
+    Jref = o.jacobian(P, phi, conp=conp)
+    ev = evaluator(name)
+    x = phi if order == "C" else phi.T
+    out = ev.jacobian(to_dev(P, cuda_device), to_dev(x, cuda_device), order=order, conp=conp,
+                      jac_format=fmt).cpu().numpy()
+    assert np.isfinite(out).all()
+    J = _dense_from(out, order, fmt, mech, ev, n)
+    if fmt == "sparse":
+        # entries outside the pattern are not stored; compare on the pattern
+        mask = np.zeros((mech.nn, mech.nn), dtype=bool)
+        ptr, ind = ev.jacobian_indices("C")
+        for r in range(mech.nn):
+            mask[r, ind[ptr[r]:ptr[r + 1]]] = True
+        Jref = np.where(mask[None], Jref, 0.0)
+    assert row_rel_err(J, Jref) < RTOL_JAC
+
+
+def test_pywrap_kernels_match_device_api(cuda_device):
+    """PyJacobianKernel / PySpecies_RatesKernel (host arrays) equal the device path."""
+    mech = load_mech("gri30")
+    api = pkg("api")
+    n = 129
+    P, phi = states("gri30", n, 13, True)
+    for order in ("C", "F"):
+        mod = api.pywrap(mech, order=order, conp=True, jac_format="sparse")
+        x = np.ascontiguousarray(phi if order == "C" else phi.T)
+        rk = mod.PySpecies_RatesKernel(n, 4)
+        dphi = np.zeros_like(x)
+        rk(P, x, dphi)
+        jk = mod.PyJacobianKernel(n, 4)
+        jac = np.zeros(n * mech.jac_nnz())
+        jk(P, x, jac)
+        ev = evaluator("gri30")
+        d2 = ev.species_rates(to_dev(P, cuda_device), to_dev(x, cuda_device), order=order).cpu().numpy()
+        j2 = ev.jacobian(to_dev(P, cuda_device), to_dev(x, cuda_device), order=order,
+                         jac_format="sparse").cpu().numpy()
+        assert np.array_equal(dphi, d2)
+        assert np.array_equal(jac, j2.ravel())
+        assert rk.num_species() == 53 and rk.num_reactions() == 325
+        assert jk.required_working_memory() > 0
+
+
+def test_indices_bit_exact_device(cuda_device):
+    """The index arrays the C ABI returns equal the front end's (bit-exact)."""
+    for name in MECHS:
+        mech = load_mech(name)
+        ev = evaluator(name)
+        for order in ("C", "F"):
+            ptr, ind = ev.jacobian_indices(order)
+            eptr, eind = mech.pattern(order)
+            assert np.array_equal(ptr, eptr) and np.array_equal(ind, eind)
