@@ -23,6 +23,7 @@
 
 namespace {
 
+constexpr int PJG_KIND_VJP = 2;  // internal kernel kind of pjg_vjp
 thread_local char g_err[512] = "";
 // kernel launches issued by this library, and optional per-launch timing of
 // the evaluation kernels (pjg_profile_begin / pjg_profile_end)
@@ -197,7 +198,7 @@ int build_slots(pjg_mech* m, bool F, bool sparse, SlotTables** out)
 // per-state bytes of working arrays for one evaluation
 size_t state_bytes(const pjg_mech* m, int kind, bool c_order_jac, int nslot)
 {
-    size_t arrs = kind == PJG_JACOBIAN ? ARR_N_JAC : ARR_N_RATES;
+    size_t arrs = kind == PJG_SPECIES_RATES ? ARR_N_RATES : ARR_N_JAC;
     size_t b = arrs * m->ns * sizeof(double);
     if (kind == PJG_JACOBIAN && c_order_jac) b += (size_t)nslot * sizeof(double);
     return b;
@@ -243,7 +244,8 @@ void fill_common(const pjg_mech* m, EvalArgs& a)
 }
 
 int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_format,
-             const double* param, const double* phi, double* out, cudaStream_t st)
+             const double* param, const double* phi, double* out, cudaStream_t st,
+             const double* v = nullptr)
 {
     if (!m) return fail(PJG_ERR_ARG, "null mechanism");
     if (n < 0) return fail(PJG_ERR_ARG, "negative problem size");
@@ -252,6 +254,7 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
         return fail(PJG_ERR_ARG, "jac_format must be 0 (full) or 1 (sparse)");
     if (n == 0) return 0;
     if (!param || !phi || !out) return fail(PJG_ERR_ARG, "null array");
+    if (kind == PJG_KIND_VJP && !v) return fail(PJG_ERR_ARG, "null vector");
     const bool F = order == 'F';
     const int NN = m->nn;
     SlotTables* t = nullptr;
@@ -291,6 +294,9 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
             a.dphi = F ? out + off : out + off * NN;
             a.dphi_ss = a.phi_ss;
             a.dphi_sj = a.phi_sj;
+        } else if (kind == PJG_KIND_VJP) {
+            a.v = F ? v + off : v + off * NN;
+            a.vjp = F ? out + off : out + off * NN;
         } else {
             a.nslot = t->nslot;
             if (F) {
@@ -548,9 +554,7 @@ int pjg_jacobian(pjg_mech* m, int64_t n, char order, int conp, int jac_format, c
 int pjg_vjp(pjg_mech* m, int64_t n, char order, int conp, const double* param, const double* phi,
             const double* v, double* out, void* stream)
 {
-    (void)m; (void)n; (void)order; (void)conp; (void)param; (void)phi; (void)v; (void)out;
-    (void)stream;
-    return fail(PJG_ERR_UNSUPPORTED, "pjg_vjp not available in this build");
+    return run_eval(m, PJG_KIND_VJP, n, order, conp, 0, param, phi, out, (cudaStream_t)stream, v);
 }
 
 int pjg_kernel_create(pjg_mech* m, int kind, size_t problem_size, size_t work_size, char order,

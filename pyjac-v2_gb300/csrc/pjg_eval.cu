@@ -85,13 +85,15 @@ struct FallState {
 #define PJG_JAC_MINB 3  // resident 128-thread blocks per SM requested for the Jacobian kernel
 #endif
 
-template <int KIND>  // 0 species rates, 1 Jacobian
-__global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
+template <int KIND>  // 0 species rates, 1 Jacobian, 2 J^T v
+__global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND == 2 ? 3 : 4))
     eval_kernel(const EvalArgs a)
 {
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.n) return;  // no block-wide synchronisation below
     constexpr bool JAC = KIND == 1;
+    constexpr bool VJP = KIND == 2;
+    constexpr bool DER = KIND >= 1;  // derivative terms needed
     extern __shared__ double smem[];
     const int ns = a.ns, last = ns - 1;
     auto arr = [&](int which) -> SV {
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
     SV conc = arr(ARR_CONC), bk = arr(ARR_B), wdot = arr(ARR_WDOT);
     SV db{nullptr, 0}, nsrow{nullptr, 0}, hw{nullptr, 0}, cpa{nullptr, 0}, dcpa{nullptr, 0},
         ha{nullptr, 0};
-    if (JAC) {
+    if (DER) {
         db = arr(ARR_DB);
         nsrow = arr(ARR_NSROW);
         hw = arr(ARR_HW);
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
     const double P = conp ? prm : E;
     const double Vinv = 1.0 / fmax(1e-30, V);
     const double logP = a.need_logP ? log(P) : 0.0;
-    const double Tjinv = JAC ? 1.0 / T : 0.0;
+    const double Tjinv = DER ? 1.0 / T : 0.0;
     const double rt_inv = 1.0 / (RU * T);  // unclamped, as the reference's thd concentration
     const double PoRT = P * rt_inv;
 
@@ -132,14 +134,14 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
         nsum = nsum + nk;
         conc[k] = nk * Vinv;
         wdot[k] = 0.0;
-        if (JAC) nsrow[k] = 0.0;
+        if (DER) nsrow[k] = 0.0;
     }
     conc[last] = P / (RU * Tc) + -1.0 * fmax(SMALL, nsum) * Vinv;
     wdot[last] = 0.0;
 
     // thermo: Gibbs functions for Kc (+ derivatives and cp, h for the Jacobian)
     double h_ns = 0.0, cp_ns = 0.0, dcp_ns = 0.0;
-    if (JAC) {
+    if (DER) {
         const Thermo tl = thermo<true>(a.sp + (int64_t)last * PJG_SP_DOUBLES, Tc, logT, Tinv, conp);
         h_ns = tl.h;
         cp_ns = tl.cp;
@@ -159,6 +161,28 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
     } else {
         for (int k = 0; k < ns; ++k)
             bk[k] = thermo<false>(a.sp + (int64_t)k * PJG_SP_DOUBLES, Tc, logT, Tinv, conp).b;
+    }
+
+    // J^T v: rows T and E of J are linear in the species rows, so v folds into
+    // species weights vt_k = v_k + alpha * hw_k + beta * (1 - W_k/W_ns) known
+    // before the reaction pass (cp_tot needs no rates); vt overwrites hw and the
+    // species part of the product accumulates in nsrow.
+    double vt_c0 = 0.0, v1 = 0.0, vout0 = 0.0, vout1 = 0.0, vNS = 0.0, cp_tot_v = 0.0;
+    if (VJP) {
+        const double* vv = a.v + s * a.phi_ss;
+        const double v0 = vv[0];
+        v1 = vv[a.phi_sj];
+        double ct = 0.0;
+        for (int k = 0; k < last; ++k) ct = fma(conc[k], cpa[k], ct);
+        ct = fma(conc[last], cp_ns, ct);
+        cp_tot_v = ct;
+        const double extra = conp ? V : P, fixed = conp ? P : V;
+        vt_c0 = v0 + v1 * extra * Tjinv;
+        const double alpha = -vt_c0 / (V * ct), beta = v1 * T * RU / fixed;
+        for (int k = 0; k < last; ++k) {
+            const double omw = ldg(a.sp + (int64_t)k * PJG_SP_DOUBLES + SP_OMW);
+            hw[k] = vv[(int64_t)(2 + k) * a.phi_sj] + alpha * hw[k] + beta * omw;
+        }
     }
 
     // ---------------------------------------------------------------- reactions
@@ -183,7 +207,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
         double kf, dlnkf_dT = 0.0, dlnkf_dlnP = 0.0;
         if (form <= FORM_ARR) {
             kf = arrhenius(form, ldg(p + P_A), ldg(p + P_B), ldg(p + P_TA), bint, Tc, logT, Tinv);
-            if (JAC) dlnkf_dT = (ldg(p + P_B) + ldg(p + P_TA) * Tjinv) * Tjinv;
+            if (DER) dlnkf_dT = (ldg(p + P_B) + ldg(p + P_TA) * Tjinv) * Tjinv;
         } else if (form == FORM_PLOG) {
             kf = gexp(plog_logk(a.aux + auxo, logT, Tinv, logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP));
         } else {
@@ -202,7 +226,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
                 const int nu = ent_nur(ent[e]) - ent_nuf(ent[e]);
                 if (nu != 0) {
                     Bsum = addnu(Bsum, nu, bk[ent_spec(ent[e])]);
-                    if (JAC) dB = addnu(dB, nu, db[ent_spec(ent[e])]);
+                    if (DER) dB = addnu(dB, nu, db[ent_spec(ent[e])]);
                 }
             }
             kr = kf * ldg(p + P_PSUM) * exp(-fmin(EXP_MAX, Bsum));
@@ -288,11 +312,10 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
                 wdot[ent_spec(ent[e])] = addnu(wv[e], ent_nur(ent[e]) - ent_nuf(ent[e]), net);
             }
         }
-        if (!JAC) continue;
+        if (!DER) continue;
 
         // ------------------------------------------------- Jacobian terms
-        const int so = __ldg(a.rxn_slot_off + i);
-        const int* slots = a.rxn_slots + so;
+        const int* slots = JAC ? a.rxn_slots + __ldg(a.rxn_slot_off + i) : nullptr;
         const double kr_ = rev ? kr : 0.0;
         double cg[PJG_MAXSP];
 #pragma unroll
@@ -419,6 +442,41 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
         }
         const double cns = ldg(p + P_CNS);
         const bool nslist = flags & RX_NSLIST;
+        if (VJP) {
+            // w = sum_k nu_k vt_k over the species rows of this reaction
+            double w = 0.0;
+#pragma unroll
+            for (int ka = 0; ka < PJG_MAXSP; ++ka) {
+                if (ka >= nsp) break;
+                const int k = ent_spec(ent[ka]);
+                if (k == last) continue;
+                w = addnu(w, ent_nur(ent[ka]) - ent_nuf(ent[ka]), hw[k]);
+            }
+            if (w != 0.0) {
+                const double wc = w * ci_;
+                double vo[PJG_MAXSP];
+#pragma unroll
+                for (int jb = 0; jb < PJG_MAXSP; ++jb)
+                    if (jb < nsp && ent_spec(ent[jb]) != last) vo[jb] = nsrow[ent_spec(ent[jb])];
+#pragma unroll
+                for (int jb = 0; jb < PJG_MAXSP; ++jb) {
+                    if (jb >= nsp) break;
+                    if (ent_spec(ent[jb]) != last) nsrow[ent_spec(ent[jb])] = fma(wc, g[jb], vo[jb]);
+                }
+                if (hasns) vNS = fma(wc, gns, vNS);
+                if (thd) {
+                    const double wx = w * X;
+                    for (int l = 0; l < thd_cnt; ++l) {
+                        const int j = __ldg(a.thd_spec + thd_off + l);
+                        if (j != last) nsrow[j] = fma(__ldg(a.thd_coef + thd_off + l), wx, nsrow[j]);
+                    }
+                    if (nslist) vNS = fma(cns, wx, vNS);
+                }
+                vout0 = fma(w, d0, vout0);
+                vout1 = fma(w, d1, vout1);
+            }
+            continue;
+        }
         // scatter into the species rows of this reaction
 #pragma unroll
         for (int ka = 0; ka < PJG_MAXSP; ++ka) {
@@ -464,7 +522,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
 
     // ------------------------------------------- temperature and E rates
     double upper = 0.0, lower = 0.0;
-    if (JAC) {
+    if (DER) {
         for (int k = 0; k < last; ++k) {
             lower = fma(conc[k], cpa[k], lower);
             upper = fma(ha[k], wdot[k], upper);
@@ -496,6 +554,37 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : 4)
         o[0] = Tdot;
         o[a.dphi_sj] = Edot;
         for (int k = 0; k < last; ++k) o[(int64_t)(2 + k) * a.dphi_sj] = Vval * wdot[k];
+    }
+    if (VJP) {
+        // constant parts of columns T and E (from rows T, E of dTdot_dT :1847,
+        // dEdotdT :2001, dTdotdE :1595, dEdotdE :1740) and the species columns'
+        // bath-gas and d cp_tot / dn_j terms
+        const double extra = conp ? V : P;
+        double dTsum = (cp_ns * Tjinv - dcp_ns) * conc[last];
+        double wsum = 0.0, omws = 0.0, dTsum1 = 0.0, hws = 0.0;
+        for (int k = 0; k < last; ++k) {
+            const double* rec = a.sp + (int64_t)k * PJG_SP_DOUBLES;
+            const double mw = ldg(rec + SP_MW), omw = ldg(rec + SP_OMW);
+            const double wk = wdot[k], ck = conc[k], cpk = cpa[k];
+            dTsum = dTsum + (cp_ns * Tjinv - dcpa[k]) * ck;
+            wsum = wsum + wk * (-cpk + mw * cp_ns);
+            omws = fma(omw, wk, omws);
+            dTsum1 = dTsum1 + (cpk - cp_ns) * ck;
+            hws = fma(ha[k] - h_ns * mw, wk, hws);
+        }
+        const double ct = cp_tot_v;
+        double C0 = vt_c0 * (Tdot * dTsum + wsum) / ct - v1 * extra * Tdot * Tjinv * Tjinv +
+                    v1 * RU * (conp ? V / P : 1.0) * omws;
+        double C1 = conp ? vt_c0 * (Tdot * dTsum1 + hws) / (ct * V)
+                         : -vt_c0 * Tdot * cp_ns * rt_inv / ct;
+        C1 += v1 * Tdot * Tjinv;
+        const double gam = -vt_c0 * Tdot / (V * ct);
+        double* o = a.vjp + s * a.phi_ss;
+        o[0] = vout0 + C0;
+        o[a.phi_sj] = vout1 + C1;
+        for (int j = 0; j < last; ++j)
+            o[(int64_t)(2 + j) * a.phi_sj] = nsrow[j] - vNS + gam * (cpa[j] - cp_ns);
+        return;
     }
     if (!JAC) return;
 
@@ -590,6 +679,11 @@ int pjg_launch_eval(const EvalArgs& a, int kind, void* stream, size_t smem_bytes
             cudaFuncSetAttribute(eval_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem_bytes);
         eval_kernel<1><<<grid, PJG_BLOCK, smem_bytes, st>>>(a);
+    } else if (kind == 2) {
+        if (smem_bytes > 48 * 1024)
+            cudaFuncSetAttribute(eval_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem_bytes);
+        eval_kernel<2><<<grid, PJG_BLOCK, smem_bytes, st>>>(a);
     } else {
         if (smem_bytes > 48 * 1024)
             cudaFuncSetAttribute(eval_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
