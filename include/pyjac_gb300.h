@@ -113,6 +113,29 @@ int pjg_kernel_call(pjg_kernel* k, const double* param, const double* phi, doubl
 int pjg_kernel_required_memory(const pjg_kernel* k, size_t* bytes);
 int pjg_kernel_destroy(pjg_kernel* k);
 
+/* Surrogate network building blocks (no reference counterpart: the learned
+ * wdot surrogate beside the FP64 path).  Operands are BF16 (raw 16-bit
+ * storage, row-major, leading dimensions in elements, multiples of 8, 16-byte
+ * aligned); products accumulate in FP32 on the tcgen05 tensor cores.
+ *
+ * pjg_mlp_linear: Y = act(X W^T + b) for X [M x K] and W [N x K]
+ * (32 <= N <= 256, N % 32 == 0; 16 <= K <= 256, K % 16 == 0).  act 1 = SiLU.
+ * When zprev is given (input-gradient pass) the product is multiplied by
+ * SiLU'(zprev) before act.  Optional outputs: Y (BF16), YT (BF16, transposed,
+ * YT[n * ldyt + m]), Z (BF16 pre-activation), Y32 (FP32), colsum (FP32,
+ * += column sums of the result; bias gradients).
+ * pjg_mlp_wgrad: C [Mo x No] += A [Mo x Kb] B [No x Kb]^T (FP32 C; Kb % 64 == 0),
+ * the weight gradient reduced over states.
+ * pjg_mlp_status: 1 if a tensor-core kernel timed out waiting for its
+ * accumulator since the last clear. */
+int pjg_mlp_linear(const void* X, int64_t ldx, const void* W, int64_t ldw, int64_t M, int N, int K,
+                   const float* bias, int act, const void* zprev, int64_t ldzp, void* Y, int64_t ldy,
+                   void* YT, int64_t ldyt, void* Z, int64_t ldz, float* Y32, int64_t ldy32,
+                   float* colsum, void* stream);
+int pjg_mlp_wgrad(const void* A, int64_t lda, const void* B, int64_t ldb, int Mo, int No,
+                  int64_t Kb, float* C, int64_t ldc, void* stream);
+int pjg_mlp_status(int clear);
+
 /* Copy the last error message of this thread into buf (always NUL-terminated). */
 int pjg_last_error(char* buf, size_t len);
 

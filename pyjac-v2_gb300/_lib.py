@@ -42,6 +42,14 @@ SIGNATURES = [
     ("pjg_kernel_required_memory", ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_size_t)]),
     ("pjg_kernel_destroy", ctypes.c_int, [_VP]),
     ("pjg_last_error", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
+    ("pjg_mlp_linear", ctypes.c_int,
+     [_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int, _VP,
+      ctypes.c_int, _VP, ctypes.c_int64, _VP, ctypes.c_int64, _VP, ctypes.c_int64, _VP,
+      ctypes.c_int64, _VP, ctypes.c_int64, _VP, _VP]),
+    ("pjg_mlp_wgrad", ctypes.c_int,
+     [_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, _VP,
+      ctypes.c_int64, _VP]),
+    ("pjg_mlp_status", ctypes.c_int, [ctypes.c_int]),
     ("pjg_launch_count", ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
     ("pjg_fp64_peak", ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     ("pjg_profile_begin", ctypes.c_int, []),

@@ -20,6 +20,7 @@
 
 #include "../../include/pyjac_gb300.h"
 #include "pjg_eval.cuh"
+#include "pjg_mlp.cuh"
 
 namespace {
 
@@ -361,6 +362,38 @@ int pjg_last_error(char* buf, size_t len)
     snprintf(buf, len, "%s", g_err);
     return 0;
 }
+
+int pjg_mlp_linear(const void* X, int64_t ldx, const void* W, int64_t ldw, int64_t M, int N, int K,
+                   const float* bias, int act, const void* zprev, int64_t ldzp, void* Y, int64_t ldy,
+                   void* YT, int64_t ldyt, void* Z, int64_t ldz, float* Y32, int64_t ldy32,
+                   float* colsum, void* stream)
+{
+    if (M < 0) return fail(PJG_ERR_ARG, "negative row count");
+    const int rc = mlp_launch_rows(X, ldx, W, ldw, M, N, K, bias, act, zprev, ldzp, Y, ldy, YT, ldyt,
+                                   Z, ldz, Y32, ldy32, colsum, stream);
+    if (rc == -1)
+        return fail(PJG_ERR_ARG, "pjg_mlp_linear: unsupported shape or misaligned operand "
+                                 "(N %% 32, K %% 16, N, K <= 256, leading dims %% 8, 16-byte aligned)");
+    if (rc) return fail(PJG_ERR_CUDA, "pjg_mlp_linear launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+    g_launches.fetch_add(1);
+    return 0;
+}
+
+int pjg_mlp_wgrad(const void* A, int64_t lda, const void* B, int64_t ldb, int Mo, int No, int64_t Kb,
+                  float* C, int64_t ldc, void* stream)
+{
+    const int rc = mlp_launch_wgrad(A, lda, B, ldb, Mo, No, Kb, C, ldc, stream);
+    if (rc == -1)
+        return fail(PJG_ERR_ARG, "pjg_mlp_wgrad: unsupported shape or misaligned operand "
+                                 "(No %% 32, No <= 256, Kb %% 64, leading dims %% 8)");
+    if (rc) return fail(PJG_ERR_CUDA, "pjg_mlp_wgrad launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+    g_launches.fetch_add(1);
+    return 0;
+}
+
+int pjg_mlp_status(int clear) { return mlp_error_flag(clear); }
 
 int pjg_fp64_peak(double* tflops)
 {
