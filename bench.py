@@ -145,6 +145,66 @@ def cpu_reference_run(mech, n_sample, steps, seed=1):
             "sample": "%d GRI-30 states per step, %s" % (n_sample, desc)}, sec
 
 
+def surrogate_bench(mech, ev, dev, n_train, epochs, n_eval, log=None):
+    """Train the BF16 surrogate on n_train states (Sobolev loss), then report its
+    error against the FP64 kernel and the wdot speedup at several tolerances on
+    n_eval fresh states (FP64 fallback included in the timed path)."""
+    import torch
+    sg = pkg("surrogate")
+    s = sg.Surrogate(mech, device=dev, evaluator=ev)
+    t0 = time.time()
+    hist = s.fit(n_train=n_train, epochs=epochs, batch=16384, lr=2e-3, log=log)
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    data = s.make_data(n_eval, seed=4242, sobolev=False)
+    P, phi = data["P"], data["phi"]
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, r
+
+    t_fp64, _ = timed(lambda: ev.species_rates(P, phi))
+    t_net, raw = timed(lambda: s.predict_raw(P, phi))
+    y_hat = raw[0]
+    err = s.rel_error(y_hat, data["y"])
+    q = torch.quantile(err[: min(len(err), 1 << 24)].float(), torch.tensor([0.5, 0.9, 0.99], device=dev))
+    qmax = torch.quantile(s.max_rel_error(y_hat, data["y"]).float(),
+                          torch.tensor([0.5, 0.9, 0.99], device=dev))
+    tols = []
+    for tol in (1e-1, 1e-2, 1e-3):
+        t_tol, (out, info) = timed(lambda: s.species_rates(P, phi, tol=tol, return_info=True), reps=1)
+        yo = torch.cat([out[:, :1], out[:, 2:]], dim=1)
+        e2 = s.rel_error(yo, data["y"])
+        tols.append({"tol": tol, "ms": t_tol, "fallback_frac": info["fallback_frac"],
+                     "speedup_vs_fp64": t_fp64 / t_tol,
+                     "frac_states_within_tol": float((e2 <= tol).float().mean()),
+                     "p99_err": float(torch.quantile(e2.float(), 0.99))})
+    return {"network": "54 -> 4x256 SiLU -> 53 (+1 error estimate), BF16 weights/activations, "
+                       "FP32 accumulate, tcgen05 GEMMs",
+            "train_states": n_train, "epochs": epochs, "train_s": t_train,
+            "final_value_mse": hist[-1]["value_mse"], "final_sobolev_mse": hist[-1]["sobolev_mse"],
+            "eval_states": n_eval, "fp64_rates_ms": t_fp64, "network_ms": t_net,
+            "network_speedup_vs_fp64": t_fp64 / t_net,
+            "err_median": float(q[0]), "err_p90": float(q[1]), "err_p99": float(q[2]),
+            "worst_component_err_median": float(qmax[0]), "worst_component_err_p90": float(qmax[1]),
+            "frac_err_below": {"1e-1": float((err <= 1e-1).float().mean()),
+                               "1e-2": float((err <= 1e-2).float().mean()),
+                               "1e-3": float((err <= 1e-3).float().mean())},
+            "with_fallback": tols,
+            "error_metric": "per state ||(y_hat - y)/rms|| / ||y/rms|| over dT/dt and the 52 molar "
+                            "rates (rms over training states); worst component: "
+                            "max_k |y_hat - y| / (|y| + 1e-3 rms_k)"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -177,6 +237,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=16384)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--sur-train", type=int, default=1 << 22)
+    ap.add_argument("--sur-epochs", type=int, default=12)
+    ap.add_argument("--sur-eval", type=int, default=1 << 22)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -302,6 +366,13 @@ def main():
     if rank == 0 and not args.no_cpu:
         cpu, _ = cpu_reference_run(mech, args.cpu_sample, 1)
 
+    sur = None
+    if not args.no_surrogate:
+        del out
+        torch.cuda.empty_cache()
+        sur = surrogate_bench(mech, ev, dev, args.sur_train, args.sur_epochs, args.sur_eval,
+                              log=lambda h: print(json.dumps(h), file=sys.stderr))
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
@@ -313,7 +384,7 @@ def main():
                            "states": n, "order": args.order, "jac_format": args.format,
                            "conp": True, "l2": "inputs 432 MB and outputs > L2; no flush"},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": launches, "clocks": clk}
+                "gpu_launches": launches, "clocks": clk, "surrogate": sur}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -1,0 +1,99 @@
+"""Surrogate network (GPU): gradients of the tcgen05 training kernels against
+the CPU reference, a short Sobolev training run, inference with fallback, and
+what the trained network gains over the FP64 kernel alone."""
+import time
+
+import numpy as np
+import pytest
+
+from conftest import load_mech, pkg
+
+pytestmark = pytest.mark.gpu
+
+
+def test_network_gradients_match_cpu_reference(cuda_device):
+    import torch
+    import mlp_ref
+    sg = pkg("surrogate")
+    net = sg.MLP(cuda_device, seed=3)
+    for b in net.b:
+        b.normal_(0, 0.1)
+    M = 512
+    torch.manual_seed(0)
+    X = torch.randn(M, sg.NIN_P, device=cuda_device)
+    X[:, sg.NIN:] = 0
+    Xb = X.bfloat16().contiguous()
+    out = net.forward(Xb, keep=True)
+    dY = torch.randn(M, sg.NOUT_P, device=cuda_device) / M
+    gW, gb = net.backward(Xb.t().contiguous(), dY)
+    Ws = [w.cpu().numpy() for w in net.W]
+    bs = [b.cpu().numpy() for b in net.b]
+    y_ref, saved = mlp_ref.forward(Xb.float().cpu().numpy(), Ws, bs)
+    assert np.abs(out.cpu().numpy() - y_ref).max() / np.abs(y_ref).max() < 2e-2
+    rW, rb = mlp_ref.backward(dY.cpu().numpy(), Ws, saved)
+    masks = [net.mask_in.cpu().numpy()] + [1.0] * 3 + [net.mask_out.cpu().numpy()]
+    for l in range(5):
+        ref = rW[l] * masks[l]
+        err = np.linalg.norm(gW[l].cpu().numpy() - ref) / np.linalg.norm(ref)
+        assert err < 2e-2, (l, err)
+        nb = sg.ERR + 1 if l == 4 else len(rb[l])
+        errb = np.linalg.norm(gb[l].cpu().numpy()[:nb] - rb[l][:nb]) / max(np.linalg.norm(rb[l][:nb]), 1e-30)
+        assert errb < 2e-2, (l, errb)
+
+
+def test_sobolev_training_and_fallback(cuda_device):
+    import torch
+    sg = pkg("surrogate")
+    mech = load_mech("gri30")
+    s = sg.Surrogate(mech, device=cuda_device, seed=1)
+    s.make_data(1 << 14, seed=0, sobolev=False)  # normalisation of the untrained network
+    data = s.make_data(8192, seed=99, sobolev=False)
+    mse0 = s.eval_mse(data)
+    hist = s.fit(n_train=1 << 16, epochs=6, batch=4096, lr=2e-3)
+    assert hist[-1]["value_mse"] < hist[0]["value_mse"]
+    y_hat, lerr, _ = s.predict_raw(data["P"], data["phi"])
+    err = s.rel_error(y_hat, data["y"])
+    assert torch.isfinite(y_hat).all()
+    # fallback: with an impossible tolerance every state is evaluated in FP64
+    out, info = s.species_rates(data["P"], data["phi"], tol=1e-12, return_info=True)
+    assert info["fallback_frac"] == 1.0
+    assert torch.equal(out, data["dphi"])
+    # checkpoint round trip
+    import tempfile, os
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "s.npz")
+        s.save(p)
+        s2 = sg.Surrogate(mech, device=cuda_device, seed=5, evaluator=s.ev)
+        s2.load(p)
+        y2, _, _ = s2.predict_raw(data["P"], data["phi"])
+        assert torch.equal(y2, y_hat)
+    assert torch.isfinite(err).all()
+    # held-out error of the trained network below the untrained one
+    assert s.eval_mse(data) < mse0
+
+
+def test_surrogate_inference_faster_than_fp64_kernel(cuda_device):
+    """What the network gains: its forward pass over 1M states against the FP64
+    species-rate kernel over the same states."""
+    import torch
+    sg = pkg("surrogate")
+    mech = load_mech("gri30")
+    s = sg.Surrogate(mech, device=cuda_device, seed=2)
+    s.make_data(1 << 14, seed=3, sobolev=False)  # fixes the normalisation
+    n = 1 << 20
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=4, x_floor=1e-12)
+    P = torch.from_numpy(P).to(cuda_device)
+    phi = torch.from_numpy(phi).to(cuda_device)
+    for _ in range(2):
+        s.predict_raw(P, phi)
+        s.ev.species_rates(P, phi)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.predict_raw(P, phi)
+    torch.cuda.synchronize()
+    t_net = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s.ev.species_rates(P, phi)
+    torch.cuda.synchronize()
+    t_fp64 = time.perf_counter() - t0
+    assert t_net < t_fp64, (t_net, t_fp64)
