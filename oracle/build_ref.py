@@ -40,14 +40,77 @@ def _sizes(exdir):
     return rwk, (rwk - off) // 128
 
 
+_QUOTED = re.compile(r'^\s*#\s*include\s*"([^"]+)"', re.M)
+
+
+def _bundle(path, dirs, seen=None):
+    """Text of `path` with every quoted #include inlined from `dirs` (each file
+    once, as its include guard would have it); system (<...>) includes stay as
+    they are, so that the result compiles against the headers of whichever
+    host builds it."""
+    seen = set() if seen is None else seen
+    seen.add(os.path.realpath(path))
+    with open(path) as f:
+        text = f.read()
+
+    def sub(m):
+        for d in [os.path.dirname(path)] + dirs:
+            q = os.path.join(d, m.group(1))
+            if os.path.exists(q):
+                if os.path.realpath(q) in seen:
+                    return ""
+                return _bundle(q, dirs, seen)
+        raise FileNotFoundError(m.group(1))
+    return _QUOTED.sub(sub, text)
+
+
+def _compile_tu(tu, so, quiet):
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-w", "-x", "c++", tu,
+           "-o", so]
+    if not quiet:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+
+
+def build_from_preprocessed(quiet=True):
+    """Where the reference tree is absent (the aarch64 GPU host), compile the
+    preprocessed translation units this recipe left in oracle/_ref/."""
+    built = {}
+    for mech in MECHS:
+        tu = os.path.join(OUT, "ref_%s.ii" % mech)
+        so = os.path.join(OUT, "libref_%s.so" % mech)
+        if not os.path.exists(tu):
+            continue
+        if not (os.path.exists(so) and os.path.getmtime(so) >= os.path.getmtime(tu)):
+            try:
+                _compile_tu(tu, so, quiet)
+            except (OSError, subprocess.CalledProcessError):
+                continue
+        built[mech] = so
+    return built
+
+
 def build(reference="/root/reference", quiet=False):
-    """Compile every shipped example; return {mech: path_to_so}."""
+    """Compile every shipped example; return {mech: path_to_so}.
+
+    Also writes oracle/_ref/ref_<mech>.ii, the shim with the example's
+    generated code inlined (a build intermediate, not committed),
+    so that hosts without the reference tree can build the same library with
+    build_from_preprocessed()."""
+    if not os.path.isdir(os.path.join(reference, "examples", "opencl")):
+        return build_from_preprocessed(quiet)
     os.makedirs(OUT, exist_ok=True)
     built = {}
     for mech in MECHS:
         exdir = os.path.join(reference, "examples", "opencl", mech)
         if not os.path.isdir(exdir):
             continue
+        tu = os.path.join(OUT, "ref_%s.ii" % mech)
+        rwk, jac = _sizes(exdir)
+        with open(tu, "w") as f:
+            f.write("#define REF_RWK %d\n#define REF_JAC_SIZE %d\n" % (rwk, jac))
+            f.write(_bundle(os.path.join(HERE, "ref_shim", "ref_driver.cpp"),
+                            [os.path.join(HERE, "ref_shim"), exdir]))
         so = os.path.join(OUT, "libref_%s.so" % mech)
         src = os.path.join(HERE, "ref_shim", "ref_driver.cpp")
         deps = [src, os.path.join(HERE, "ref_shim", "cl_shim.h")] + [

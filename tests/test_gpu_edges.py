@@ -1,0 +1,122 @@
+"""GPU edge cases against the oracle: empty and single-state batches, states at
+and beyond the guards' limits, exact-zero moles, and problems that span more
+than one launch chunk of the working buffer.
+
+The guards are pyJac's (pyjac/core/instruction_creator.py:370-478): rates use
+T clamped to [100, 10000] K, moles floored at 1e-300 in the concentration
+products, exp arguments clamped at 690.775527898; the explicit T, V, P factors
+of the Jacobian use the unclamped state.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_mech, oracle_mod, pkg, row_rel_err
+
+pytestmark = pytest.mark.gpu
+
+RTOL_RATES = 1e-10
+RTOL_JAC = 1e-8
+
+
+def _dev(a, device):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device)
+
+
+def _rates_err(d, ref, scale):
+    den = np.abs(ref) + scale
+    diff = np.abs(d - ref)
+    return float(np.where(den > 0, diff / np.where(den > 0, den, 1.0),
+                          np.where(diff > 0, np.inf, 0.0)).max())
+
+
+def _check(ev, mech, P, phi, order, conp, device):
+    o = oracle_mod().Oracle(mech)
+    ref = o.species_rates(P, phi, conp=conp)
+    scale = o.rates_scale(P, phi, conp=conp)
+    x = phi if order == "C" else phi.T
+    d = ev.species_rates(_dev(P, device), _dev(x, device), order=order, conp=conp).cpu().numpy()
+    d = d if order == "C" else d.T
+    assert np.isfinite(d).all()
+    assert _rates_err(d, ref, scale) < RTOL_RATES
+    n, NN = phi.shape
+    out = ev.jacobian(_dev(P, device), _dev(x, device), order=order, conp=conp).cpu().numpy()
+    J = out.reshape(n, NN, NN) if order == "C" else out.reshape(NN, NN, n).transpose(2, 1, 0)
+    assert np.isfinite(J).all()
+    assert row_rel_err(J, o.jacobian(P, phi, conp=conp)) < RTOL_JAC
+
+
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_empty_batch_writes_nothing(cuda_device, order):
+    import torch
+    mech = load_mech("gri30")
+    ev = pkg("api").Evaluator(mech)
+    P = torch.zeros(0, dtype=torch.float64, device=cuda_device)
+    phi = torch.zeros((0, mech.nn) if order == "C" else (mech.nn, 0), dtype=torch.float64,
+                      device=cuda_device)
+    assert ev.species_rates(P, phi, order=order).numel() == 0
+    assert ev.jacobian(P, phi, order=order).numel() == 0
+    assert ev.vjp(P, phi, phi, order=order).numel() == 0
+
+
+@pytest.mark.parametrize("order", ["C", "F"])
+@pytest.mark.parametrize("conp", [True, False])
+def test_single_state(cuda_device, order, conp):
+    mech = load_mech("gri30")
+    P, phi = pkg("states").draw_states(mech.n_species, 1, seed=5, x_floor=1e-12, conp=conp)
+    _check(pkg("api").Evaluator(mech), mech, P, phi, order, conp, cuda_device)
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30"])
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_temperatures_at_and_beyond_the_limits(cuda_device, name, order):
+    """T below the 100 K clamp, across the NASA-7 switch at T_mid, up to and
+    beyond the 10,000 K clamp."""
+    mech = load_mech(name)
+    temps = np.array([80.0, 100.0, 100.5, 300.0, 999.999999, 1000.0, 1000.000001, 2500.0,
+                      3500.0, 6000.0, 9999.0, 10000.0, 12000.0])
+    P, phi = pkg("states").draw_states(mech.n_species, temps.size, seed=21, x_floor=1e-12)
+    # keep the composition and pressure, move T (moles follow the ideal gas law)
+    phi = phi.copy()
+    phi[:, 2:] *= (phi[:, 0] / temps)[:, None]
+    phi[:, 0] = temps
+    _check(pkg("api").Evaluator(mech), mech, P, phi, order, True, cuda_device)
+
+
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_exact_zero_moles(cuda_device, order):
+    """Species with exactly zero moles exercise the 1e-300 floors."""
+    mech = load_mech("gri30")
+    P, phi = pkg("states").draw_states(mech.n_species, 257, seed=8, x_floor=1e-12)
+    phi = phi.copy()
+    rng = np.random.default_rng(8)
+    zero = rng.random(phi[:, 2:].shape) < 0.5
+    phi[:, 2:][zero] = 0.0
+    phi[0, 2:] = 0.0  # bath gas only
+    _check(pkg("api").Evaluator(mech), mech, P, phi, order, True, cuda_device)
+
+
+@pytest.mark.parametrize("order,n", [("C", 40000), ("F", 290000)])
+def test_problem_spanning_several_launch_chunks(cuda_device, order, n):
+    """The working buffer is capped, so large batches run as several launches
+    (GRI dense: 39,552 states per launch in C order, 281,344 in F order).
+    States on both sides of each boundary must match the oracle."""
+    import torch
+    mech = load_mech("gri30")
+    NN = mech.nn
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=31, x_floor=1e-12)
+    ev = pkg("api").Evaluator(mech)
+    x = phi if order == "C" else phi.T
+    out = ev.jacobian(_dev(P, cuda_device), _dev(x, cuda_device), order=order)
+    pick = np.r_[0:64, 39488:39616, n - 64:n] if order == "C" else np.r_[0:64, 281280:281408,
+                                                                          n - 64:n]
+    idx = torch.from_numpy(pick).to(cuda_device)
+    if order == "C":
+        J = out.view(n, NN, NN).index_select(0, idx).cpu().numpy()
+    else:
+        J = out.view(NN, NN, n).index_select(2, idx).cpu().numpy().transpose(2, 1, 0)
+    del out
+    torch.cuda.empty_cache()
+    Jref = oracle_mod().Oracle(mech).jacobian(P[pick], phi[pick])
+    assert np.isfinite(J).all()
+    assert row_rel_err(J, Jref) < RTOL_JAC
