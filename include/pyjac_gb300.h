@@ -99,6 +99,18 @@ int pjg_jacobian(pjg_mech* mech, int64_t n, char order, int conp, int jac_format
  * by the torch wdot autograd.Function. */
 int pjg_vjp(pjg_mech* mech, int64_t n, char order, int conp, const double* param,
             const double* phi, const double* v, double* out, void* stream);
+/* pjg_vjp without any device allocation, for callers that cannot allocate
+ * at call time (solvers calling from a hot loop where cudaMalloc/cudaFree
+ * would synchronise the device, hosts whose pool owns all device memory).
+ * No counterpart in the reference.  Scratch is a fixed 16 MiB array inside
+ * the library on each device, held until the process exits; larger problems
+ * run as several launches on `stream`; mechanisms needing more than 16 MiB
+ * per 128 states (about 1,800 species) are rejected with PJG_ERR_ARG.  The
+ * first call on a device takes the array's address (call it before any
+ * stream capture).  All calls share the array: calls that overlap on the GPU
+ * race. */
+int pjg_vjp_noalloc(pjg_mech* mech, int64_t n, char order, int conp, const double* param,
+                    const double* phi, const double* v, double* out, void* stream);
 
 /* Kernel objects: the reference's Kernel class (kernel.hpp.in:86-335).
  * problem_size = states per call; work_size is accepted for API

@@ -34,6 +34,8 @@ SIGNATURES = [
      [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP]),
     ("pjg_vjp", ctypes.c_int,
      [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, _VP, _VP, _VP, _VP, _VP]),
+    ("pjg_vjp_noalloc", ctypes.c_int,
+     [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, _VP, _VP, _VP, _VP, _VP]),
     ("pjg_kernel_create", ctypes.c_int,
      [_VP, ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_char, ctypes.c_int,
       ctypes.c_int, ctypes.POINTER(_VP)]),

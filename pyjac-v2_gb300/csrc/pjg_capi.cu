@@ -354,6 +354,12 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
 
 }  // namespace
 
+// Internal accessors for other translation units of this library.
+int pjg_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+void pjg_internal_fill_args(const pjg_mech* m, EvalArgs* a) { fill_common(m, *a); }
+int pjg_internal_mech_ns(const pjg_mech* m) { return m->ns; }
+void pjg_internal_count_launch() { g_launches.fetch_add(1); }
+
 extern "C" {
 
 int pjg_last_error(char* buf, size_t len)
