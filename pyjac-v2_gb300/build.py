@@ -12,6 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libpyjac_gb300.so")
+STAMP = os.path.join(BUILD, "flags.txt")  # extra nvcc flags the library was built with
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -29,8 +30,14 @@ def _deps():
     return out + [os.path.abspath(__file__)]
 
 
-def up_to_date():
+def up_to_date(extra=()):
     if not os.path.exists(LIB):
+        return False
+    try:
+        with open(STAMP) as f:
+            if f.read() != " ".join(extra):
+                return False
+    except OSError:
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(d) <= t for d in _deps())
@@ -41,10 +48,11 @@ def build(force=False, verbose=False, nvcc="nvcc", extra_flags=None):
 
     ``extra_flags`` (or the PJG_NVCC_EXTRA environment variable) appends nvcc
     flags, e.g. ``-DPJG_JAC_MINB=2`` to change the Jacobian kernel's
-    launch bounds; a build with extra flags is always a full rebuild.
+    launch bounds.  The flags are recorded beside the library, so a build with
+    different flags (or none) after a variant build rebuilds everything.
     """
     extra = list(extra_flags or []) + os.environ.get("PJG_NVCC_EXTRA", "").split()
-    if not force and not extra and up_to_date():
+    if not force and up_to_date(extra):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     srcs = sources()
@@ -70,6 +78,8 @@ def build(force=False, verbose=False, nvcc="nvcc", extra_flags=None):
     if r.returncode != 0:
         raise RuntimeError("nvcc link failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(" ".join(extra))
     return LIB
 
 

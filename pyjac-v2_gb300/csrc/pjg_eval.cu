@@ -38,6 +38,7 @@
 #include <cuda_runtime.h>
 #include "pjg_eval.cuh"
 #include "pjg_math.cuh"
+#include "pjg_rxn.cuh"
 
 using namespace pjg;
 
@@ -50,39 +51,8 @@ struct SV {
     __device__ __forceinline__ double& operator[](int k) const { return b[(int64_t)k * st]; }
 };
 
-// nu * x for a warp-uniform small integer nu without an int->double conversion
-__device__ __forceinline__ double nux(int nu, double x)
-{
-    switch (nu) {
-    case 1: return x;
-    case -1: return -x;
-    case 2: return x + x;
-    case -2: return -(x + x);
-    case 0: return 0.0;
-    }
-    return (double)nu * x;
-}
-
-// acc + nu * x
-__device__ __forceinline__ double addnu(double acc, int nu, double x)
-{
-    switch (nu) {
-    case 1: return acc + x;
-    case -1: return acc - x;
-    case 2: return fma(2.0, x, acc);
-    case -2: return fma(-2.0, x, acc);
-    case 0: return acc;
-    }
-    return fma((double)nu, x, acc);
-}
-
-struct FallState {
-    double Pr, Fi, A, B, Fc, lnFc, X, lnQ, kratio;
-    double e1, e2, e3;   // Troe exponentials at the clamped temperature
-};
-
 #ifndef PJG_JAC_MINB
-#define PJG_JAC_MINB 3  // resident 128-thread blocks per SM requested for the Jacobian kernel
+#define PJG_JAC_MINB 4  // resident 128-thread blocks per SM requested for the Jacobian kernel
 #endif
 
 template <int KIND>  // 0 species rates, 1 Jacobian, 2 J^T v
@@ -126,6 +96,9 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     const double Tjinv = DER ? 1.0 / T : 0.0;
     const double rt_inv = 1.0 / (RU * T);  // unclamped, as the reference's thd concentration
     const double PoRT = P * rt_inv;
+    StateVars sv;
+    sv.T = T; sv.Tc = Tc; sv.logT = logT; sv.Tinv = Tinv; sv.Tjinv = Tjinv;
+    sv.V = V; sv.P = P; sv.PoRT = PoRT; sv.rt_inv = rt_inv; sv.logP = logP; sv.conp = conp;
 
     // concentrations (rate_subs.py get_concentrations :597-706)
     double nsum = 0.0;
@@ -187,119 +160,13 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
 
     // ---------------------------------------------------------------- reactions
     for (int i = 0; i < a.nr; ++i) {
-        const PjgRxn* R = a.rxn + i;
-        const int4 h0 = __ldg(reinterpret_cast<const int4*>(R));
-        const int4 h1 = __ldg(reinterpret_cast<const int4*>(R) + 1);
-        const int flags = h0.x, nsp = h0.y, thd_off = h0.z, thd_cnt = h0.w;
-        const int auxo = h1.x, bint = h1.z, fbint = h1.w;
-        unsigned ent[PJG_MAXSP];
-        {
-            const uint4 e0 = __ldg(reinterpret_cast<const uint4*>(R) + 2);
-            const uint4 e1 = __ldg(reinterpret_cast<const uint4*>(R) + 3);
-            ent[0] = e0.x; ent[1] = e0.y; ent[2] = e0.z; ent[3] = e0.w;
-            ent[4] = e1.x; ent[5] = e1.y; ent[6] = e1.z; ent[7] = e1.w;
-        }
-        const double* p = R->p;
-        const int form = RX_FORM(flags);
-        const bool rev = flags & RX_REV;
-
-        // forward rate constant and its log-derivatives
-        double kf, dlnkf_dT = 0.0, dlnkf_dlnP = 0.0;
-        if (form <= FORM_ARR) {
-            kf = arrhenius(form, ldg(p + P_A), ldg(p + P_B), ldg(p + P_TA), bint, Tc, logT, Tinv);
-            if (DER) dlnkf_dT = (ldg(p + P_B) + ldg(p + P_TA) * Tjinv) * Tjinv;
-        } else if (form == FORM_PLOG) {
-            kf = gexp(plog_logk(a.aux + auxo, logT, Tinv, logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP));
-        } else {
-            const double l10 = cheb_log10k(a.aux + auxo, Tinv, logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP);
-            kf = exp(LN10 * fmin(EXP_MAX, l10));
-            dlnkf_dT *= LN10;
-            dlnkf_dlnP *= LN10;
-        }
-        // reverse rate: kr = kf / Kc, Kc = (P_atm/R)^nu_sum exp(sum nu b)
-        double kr = 0.0, dB = 0.0;
-        if (rev) {
-            double Bsum = 0.0;
-#pragma unroll
-            for (int e = 0; e < PJG_MAXSP; ++e) {
-                if (e >= nsp) break;
-                const int nu = ent_nur(ent[e]) - ent_nuf(ent[e]);
-                if (nu != 0) {
-                    Bsum = addnu(Bsum, nu, bk[ent_spec(ent[e])]);
-                    if (DER) dB = addnu(dB, nu, db[ent_spec(ent[e])]);
-                }
-            }
-            kr = kf * ldg(p + P_PSUM) * exp(-fmin(EXP_MAX, Bsum));
-        }
-        // rates of progress (mass action on raw concentrations)
-        double rf = kf, rr = kr;
-#pragma unroll
-        for (int e = 0; e < PJG_MAXSP; ++e) {
-            if (e >= nsp) break;
-            const double c = conc[ent_spec(ent[e])];
-            rf = mulpow(rf, c, ent_nuf(ent[e]));
-            if (rev) rr = mulpow(rr, c, ent_nur(ent[e]));
-        }
-        // third-body / fall-off pressure modification
-        const int thd = RX_THD(flags);
-        const int blend = RX_BLEND(flags);
-        const bool chem = flags & RX_CHEM;
-        double ci = 1.0, M = 0.0;
-        FallState fs;
-        fs.Pr = 0.0; fs.Fi = 1.0; fs.A = 0.0; fs.B = 0.0; fs.Fc = 1.0; fs.lnFc = 0.0; fs.X = 0.0;
-        fs.lnQ = 0.0; fs.kratio = 0.0; fs.e1 = 0.0; fs.e2 = 0.0; fs.e3 = 0.0;
-        if (thd) {
-            M = PoRT * ldg(p + P_FLAG);
-            for (int l = 0; l < thd_cnt; ++l)
-                M = fma(__ldg(a.thd_coef + thd_off + l), conc[__ldg(a.thd_spec + thd_off + l)], M);
-            if (blend == BL_NONE) {
-                ci = M;
-            } else {
-                const double kfall = arrhenius(RX_FFORM(flags), ldg(p + P_FA), ldg(p + P_FB),
-                                               ldg(p + P_FTA), fbint, Tc, logT, Tinv);
-                fs.kratio = chem ? kf / kfall : kfall / kf;  // k0 / kinf
-                fs.Pr = M * fs.kratio;
-                if (blend == BL_TROE) {
-                    const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
-                    const double ta = ldg(p + P_F0);
-                    fs.e1 = gexp(-1.0 * Tc * ldg(p + P_F1));
-                    fs.e3 = gexp(-1.0 * Tc * ldg(p + P_F3));
-                    double Fc = ta * fs.e1 + (1.0 + -1.0 * ta) * fs.e3;
-                    if (flags & RX_T2) {
-                        fs.e2 = gexp(-1.0 * ldg(p + P_F2) * Tinv);
-                        Fc = Fc + fs.e2;
-                    }
-                    fs.lnFc = log(fmax(SMALL, Fc));
-                    const double logFc = fs.lnFc * INV_LN10;
-                    fs.B = -1.1762 * logFc + -0.14 * logPr + 0.806;
-                    fs.A = -0.67 * logFc + logPr + -0.4;
-                    fs.Fc = Fc;
-                    const double B2 = fs.B * fs.B;
-                    fs.Fi = exp(B2 / (fs.A * fs.A + B2) * fs.lnFc);
-                } else if (blend == BL_SRI) {
-                    const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
-                    fs.X = 1.0 / (logPr * logPr + 1.0);
-                    fs.e1 = gexp(-ldg(p + P_F1) * Tinv);
-                    fs.e3 = gexp(-Tc / ldg(p + P_F2));
-                    const double Q = ldg(p + P_F0) * fs.e1 + fs.e3;
-                    fs.lnQ = log(Q);
-                    double Fi = exp(fs.X * fs.lnQ);
-                    if (flags & RX_SRID) Fi = Fi * ldg(p + P_F3);
-                    if (flags & RX_SRIE) {
-                        const double e = ldg(p + P_F4);
-                        const int ie = (int)e;
-                        Fi = Fi * ((flags & RX_SRIEINT) ? (ie < 0 ? powi(Tinv, -ie) : powi(Tc, ie))
-                                                        : pow(Tc, e));
-                    }
-                    fs.Fi = Fi;
-                }
-                ci = fs.Fi / (1.0 + fs.Pr);
-                if (!chem) ci = ci * fs.Pr;
-            }
-        }
-        double Rnet = rf;
-        if (rev) Rnet = Rnet + -1.0 * rr;
-        const double net = thd ? Rnet * ci : Rnet;
+        RxnHead h;
+        load_head(a.rxn + i, h);
+        RxnTerms o;
+        rxn_terms<DER>(h, a.aux, a.thd_spec, a.thd_coef, last, sv, conc, bk, db, o);
+        const int flags = h.flags, nsp = h.nsp, thd_off = h.thd_off, thd_cnt = h.thd_cnt;
+        const unsigned* ent = h.ent;
+        const double* p = h.p;
         {
             // participants are distinct species: load all, then update
             double wv[PJG_MAXSP];
@@ -309,137 +176,17 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
 #pragma unroll
             for (int e = 0; e < PJG_MAXSP; ++e) {
                 if (e >= nsp) break;
-                wdot[ent_spec(ent[e])] = addnu(wv[e], ent_nur(ent[e]) - ent_nuf(ent[e]), net);
+                wdot[ent_spec(ent[e])] = addnu(wv[e], ent_nur(ent[e]) - ent_nuf(ent[e]), o.net);
             }
         }
         if (!DER) continue;
 
         // ------------------------------------------------- Jacobian terms
         const int* slots = JAC ? a.rxn_slots + __ldg(a.rxn_slot_off + i) : nullptr;
-        const double kr_ = rev ? kr : 0.0;
-        double cg[PJG_MAXSP];
-#pragma unroll
-        for (int e = 0; e < PJG_MAXSP; ++e) cg[e] = e < nsp ? gsmall(conc[ent_spec(ent[e])]) : 1.0;
-        // d R / d c_j for every participant j (dRopidnj :4169-4522)
-        double g[PJG_MAXSP];
-        double gns = 0.0;
-#pragma unroll
-        for (int j = 0; j < PJG_MAXSP; ++j) {
-            if (j >= nsp) break;
-            const int nfj = ent_nuf(ent[j]), nrj = ent_nur(ent[j]);
-            double gf = 0.0, gr = 0.0;
-            if (nfj) {
-                double S = nux(nfj, kf);
-#pragma unroll
-                for (int e = 0; e < PJG_MAXSP; ++e) {
-                    if (e >= nsp) break;
-                    S = mulpow(S, cg[e], ent_nuf(ent[e]) - (e == j));
-                }
-                gf = S;
-            }
-            if (rev && nrj) {
-                double S = nux(nrj, kr_);
-#pragma unroll
-                for (int e = 0; e < PJG_MAXSP; ++e) {
-                    if (e >= nsp) break;
-                    S = mulpow(S, cg[e], ent_nur(ent[e]) - (e == j));
-                }
-                gr = S;
-            }
-            g[j] = gf - gr;
-            if (ent_spec(ent[j]) == last) gns = g[j];
-        }
+        const int thd = RX_THD(flags);
         const bool hasns = flags & RX_HASNS;
-        const double ci_ = thd ? ci : 1.0;
-        // fall-off derivative pieces shared by the n, T and E columns
-        double inv1 = 0.0, dlnFi_dPr = 0.0;
-        if (thd && blend != BL_NONE) {
-            inv1 = 1.0 / (fs.Pr + 1.0);
-            if (blend == BL_TROE) {
-                const double absq = fs.A * fs.A + fs.B * fs.B;
-                dlnFi_dPr = -2.0 * fs.A * fs.B * fs.lnFc * (0.14 * fs.A + fs.B) /
-                            (fmax(SMALL, fs.Pr) * absq * absq * LN10);
-            } else if (blend == BL_SRI) {
-                const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
-                dlnFi_dPr = -2.0 * fs.X * fs.X * logPr / (fmax(SMALL, fs.Pr) * LN10) * fs.lnQ;
-            }
-        }
-        // d ci / dx given d Pr / dx = Pr theta + theta_n and the direct part of d ln Fi / dx
-        auto dci = [&](double theta, double theta_n, double direct) -> double {
-            const double dPr = fs.Pr * theta + theta_n;
-            double d = ci * (dlnFi_dPr * dPr + direct - dPr * inv1);
-            if (!chem) d = d + theta * ci + fs.Fi * theta_n * inv1;
-            return d;
-        };
-        const double dMfac = (thd && blend != BL_NONE) ? dci(0.0, fs.kratio, 0.0) : 1.0;
-        const double X = Rnet * dMfac;
-        const double mod = ldg(p + P_MOD);
-        // temperature column (dRopi_dT :2589-3108, dci_*_dT :2117-2588)
-        double d0 = rf * dlnkf_dT;
-        if (rev) d0 = d0 + -1.0 * rr * (dlnkf_dT + -1.0 * dB);
-        d0 = d0 * ci_ * V;
-        if (hasns) d0 += -gns * V * ci_ * PoRT * Tjinv;
-        // extra-variable column (dRopi_dE :1458-1594, dci_*_dE :362-880)
-        double d1 = 0.0;
-        if (conp) {
-            int nuf = -1, nur = -1;
-#pragma unroll
-            for (int e = 0; e < PJG_MAXSP; ++e) {
-                if (e >= nsp) break;
-                nuf += ent_nuf(ent[e]);
-                nur += ent_nur(ent[e]);
-            }
-            d1 = (-nux(nuf, rf) + (rev ? nux(nur, rr) : 0.0)) * ci_;
-        } else if (form >= FORM_PLOG) {
-            d1 = V * ci_ * Rnet * dlnkf_dlnP / P;
-        }
-        if (hasns) d1 += gns * ci_ * (conp ? PoRT : V * rt_inv);
-        if (thd) {
-            const double dM = -1.0 * PoRT * mod * Tjinv;
-            if (blend == BL_NONE) {
-                d0 += dM * V * Rnet;
-                if (conp) {
-                    if (thd != THD_UNITY) d1 += (mod * PoRT + -1.0 * M) * Rnet;
-                } else {
-                    d1 += V * Rnet * mod * rt_inv;
-                }
-            } else {
-                double b0, binf, Ta0, Tainf;
-                if (!chem) {
-                    binf = ldg(p + P_B); Tainf = ldg(p + P_TA);
-                    b0 = ldg(p + P_FB); Ta0 = ldg(p + P_FTA);
-                } else {
-                    b0 = ldg(p + P_B); Ta0 = ldg(p + P_TA);
-                    binf = ldg(p + P_FB); Tainf = ldg(p + P_FTA);
-                }
-                const double theta = Tjinv * (b0 + -1.0 * binf + (Ta0 + -1.0 * Tainf) * Tjinv);
-                const double theta_n = dM * fs.kratio;
-                double direct = 0.0;
-                if (blend == BL_TROE) {
-                    const double absq = fs.A * fs.A + fs.B * fs.B;
-                    const double ta = ldg(p + P_F0), t1 = ldg(p + P_F1), t2 = ldg(p + P_F2),
-                                 t3 = ldg(p + P_F3);
-                    // the explicit T derivative uses the unclamped T, as the reference
-                    const bool same = T == Tc;
-                    const double x1 = same ? fs.e1 : gexp(-1.0 * T * t1);
-                    const double x3 = same ? fs.e3 : gexp(-1.0 * T * t3);
-                    double dFc = -1.0 * ta * t1 * x1 + (ta + -1.0) * t3 * x3;
-                    if (flags & RX_T2) dFc += t2 * Tjinv * Tjinv * (same ? fs.e2 : gexp(-1.0 * t2 * Tjinv));
-                    direct = -fs.B * dFc *
-                             (2.0 * fs.A * (1.1762 * fs.A + -0.67 * fs.B) * fs.lnFc - fs.B * absq * LN10) /
-                             (fs.Fc * absq * absq * LN10);
-                } else if (blend == BL_SRI) {
-                    const double sa = ldg(p + P_F0), sb = ldg(p + P_F1), sc = ldg(p + P_F2);
-                    const double Q = sa * fs.e1 + fs.e3;
-                    const double dQ = sa * sb * Tjinv * Tjinv * fs.e1 - fs.e3 / sc;
-                    direct = fs.X * dQ / Q + ldg(p + P_F4) * Tjinv;
-                }
-                d0 += dci(theta, theta_n, direct) * V * Rnet;
-                const double modp = (conp ? (thd == THD_UNITY ? 0.0 : mod) * PoRT : mod * rt_inv) * fs.kratio;
-                const double th = conp ? -1.0 * (thd != THD_UNITY) : 0.0;
-                d1 += dci(th, modp, 0.0) * (conp ? 1.0 : V) * Rnet;
-            }
-        }
+        const double ci_ = o.ci_, X = o.X, d0 = o.d0, d1 = o.d1, gns = o.gns;
+        const double* g = o.g;
         const double cns = ldg(p + P_CNS);
         const bool nslist = flags & RX_NSLIST;
         if (VJP) {
@@ -485,34 +232,27 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
             if (k == last) continue;
             const int nuk = ent_nur(ent[ka]) - ent_nuf(ent[ka]);
             if (nuk == 0) continue;
-            // all loads of this row's accumulators first, so they are in flight together
-            double* ap[PJG_MAXSP + 2];
-            double av[PJG_MAXSP + 2];
+            // Fire-and-forget reductions (red.global.add.f64): the thread does not
+            // wait for the accumulator's old value.  Only this thread updates its
+            // state's entries, and one thread's operations on one address apply
+            // in program order, so every entry sums its reactions in a fixed order.
+            double* accs = a.acc + s;
 #pragma unroll
             for (int jb = 0; jb < PJG_MAXSP + 2; ++jb) {
                 if (jb >= nsp + 2) break;
                 const int sl = jb < nsp ? __ldg(slots + ka * nsp + jb)
                                         : __ldg(slots + nsp * nsp + 2 * ka + (jb - nsp));
-                ap[jb] = sl >= 0 ? a.acc + (int64_t)sl * a.acc_ld + s : nullptr;
-                av[jb] = sl >= 0 ? *ap[jb] : 0.0;
+                const double v = jb < nsp ? g[jb] * ci_ : (jb == nsp ? d0 : d1);
+                if (sl >= 0) atomicAdd(accs + (int64_t)sl * a.acc_ld, nux(nuk, v));
             }
-#pragma unroll
-            for (int jb = 0; jb < PJG_MAXSP; ++jb) {
-                if (jb >= nsp) break;
-                if (ap[jb]) *ap[jb] = addnu(av[jb], nuk, g[jb] * ci_);
-            }
-            if (ap[nsp]) *ap[nsp] = addnu(av[nsp], nuk, d0);
-            if (ap[nsp + 1]) *ap[nsp + 1] = addnu(av[nsp + 1], nuk, d1);
             double nsacc = 0.0;
             if (hasns) nsacc = gns * ci_;
             if (thd) {
                 const double wx = nux(nuk, X);
                 for (int l = 0; l < thd_cnt; ++l) {
                     const int sl = __ldg(slots + nsp * nsp + 2 * nsp + l * nsp + ka);
-                    if (sl >= 0) {
-                        double& r = a.acc[(int64_t)sl * a.acc_ld + s];
-                        r = fma(__ldg(a.thd_coef + thd_off + l), wx, r);
-                    }
+                    if (sl >= 0)
+                        atomicAdd(accs + (int64_t)sl * a.acc_ld, __ldg(a.thd_coef + thd_off + l) * wx);
                 }
                 if (nslist) nsacc = fma(cns, X, nsacc);
             }
@@ -591,6 +331,9 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     // ------------------------------------------- assemble rows T and E
     double* acc = a.acc + s;
     const int64_t ld = a.acc_ld;
+    // the reductions are performed in L2: read the accumulator there
+    __threadfence();
+    auto accr = [&](int64_t sl) { return __ldcg(acc + sl * ld); };
     // bath-gas terms: subtract the per-row sums from every species column
     for (int k = 0; k < last; ++k) {
         const double v = nsrow[k];
@@ -598,7 +341,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         const int r0 = __ldg(a.row_off + k), r1 = __ldg(a.row_off + k + 1);
         for (int q = r0; q < r1; ++q) {
             const int2 e = __ldg(a.row_list + q);
-            acc[(int64_t)e.y * ld] -= v;
+            acc[(int64_t)e.y * ld] = accr(e.y) - v;
         }
     }
     const double cp_tot = lower;
@@ -610,7 +353,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         const int c0 = __ldg(a.col_off + j), c1 = __ldg(a.col_off + j + 1);
         for (int q = c0; q < c1; ++q) {
             const int2 e = __ldg(a.col_list + q);
-            const double Jkj = acc[(int64_t)e.y * ld];
+            const double Jkj = accr(e.y);
             sum = fma(hw[e.x], Jkj, sum);
             sumE = fma(ldg(a.sp + (int64_t)e.x * PJG_SP_DOUBLES + SP_OMW), Jkj, sumE);
         }
@@ -626,8 +369,8 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         const double* rec = a.sp + (int64_t)k * PJG_SP_DOUBLES;
         const double mw = ldg(rec + SP_MW), omw = ldg(rec + SP_OMW);
         const int sl0 = __ldg(a.sp_slots + 2 * k), sl1 = __ldg(a.sp_slots + 2 * k + 1);
-        const double Jk0 = sl0 >= 0 ? acc[(int64_t)sl0 * ld] : 0.0;
-        const double Jk1 = sl1 >= 0 ? acc[(int64_t)sl1 * ld] : 0.0;
+        const double Jk0 = sl0 >= 0 ? accr(sl0) : 0.0;
+        const double Jk1 = sl1 >= 0 ? accr(sl1) : 0.0;
         const double wk = wdot[k], ck = conc[k], cpk = cpa[k], hwk = hw[k];
         rate_sum = rate_sum + Vjinv * Jk0 * (-1.0 * hwk);
         rate_sum = rate_sum + wk * (-cpk + mw * cp_ns);

@@ -1,0 +1,347 @@
+// Per-reaction evaluation of the evaluation kernels (pjg_eval.cu).
+//
+// rxn_terms() evaluates one reaction at one state: forward rate constant
+// (get_simple_arrhenius_rates :2642, PLOG :2084, Chebyshev :1904 of
+// pyjac/core/rate_subs.py), reverse rate through the equilibrium constant
+// (:1627), mass-action rates of progress (:1170-1509), third-body and
+// fall-off pressure modification (:1510-1626, :1788-2641), and, when DER is
+// set, the reaction's analytical derivative terms (create_jacobian.py
+// dRopi_dnj :4169-4522, dci_*_dnj :3558-4168, dRopidT :2589-3108,
+// dRopidE :1458-1594, dci_*_dT :2117-2588, dci_*_dE :362-880).
+//
+// The caller owns the accumulation: species rates get nu_k * net, species row
+// k of the Jacobian gets nu_k * (g_j ci) in column j, nu_k * d0 in column T,
+// nu_k * d1 in column E, nu_k * coef_l * X in the columns of the third-body
+// list, and nu_k * (gns ci + cns X) in every species column (the bath-gas
+// terms, gathered per row).
+//
+// Per-state arrays are read through an accessor with operator[] (a strided
+// view of global memory, or a shared-memory pointer).
+#pragma once
+#include "pjg_math.cuh"
+#include "pjg_tables.cuh"
+
+namespace pjg {
+
+// nu * x for a warp-uniform small integer nu without an int->double conversion
+__device__ __forceinline__ double nux(int nu, double x)
+{
+    switch (nu) {
+    case 1: return x;
+    case -1: return -x;
+    case 2: return x + x;
+    case -2: return -(x + x);
+    case 0: return 0.0;
+    }
+    return (double)nu * x;
+}
+
+// acc + nu * x
+__device__ __forceinline__ double addnu(double acc, int nu, double x)
+{
+    switch (nu) {
+    case 1: return acc + x;
+    case -1: return acc - x;
+    case 2: return fma(2.0, x, acc);
+    case -2: return fma(-2.0, x, acc);
+    case 0: return acc;
+    }
+    return fma((double)nu, x, acc);
+}
+
+// scalars of one thermochemical state used by every reaction
+struct StateVars {
+    double T;       // temperature (unclamped: explicit factors of the Jacobian)
+    double Tc;      // T clamped to [100, 10000] K (rate evaluation)
+    double logT, Tinv;  // of Tc
+    double Tjinv;   // 1 / T
+    double V, P;
+    double PoRT;    // P / (R T)
+    double rt_inv;  // 1 / (R T)
+    double logP;    // ln P (PLOG / Chebyshev mechanisms only)
+    bool conp;
+};
+
+// decoded reaction header
+struct RxnHead {
+    int flags, nsp, thd_off, thd_cnt, auxo, bint, fbint;
+    unsigned ent[PJG_MAXSP];
+    const double* p;
+};
+
+__device__ __forceinline__ void load_head(const PjgRxn* R, RxnHead& h)
+{
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(R));
+    const int4 h1 = __ldg(reinterpret_cast<const int4*>(R) + 1);
+    h.flags = h0.x;
+    h.nsp = h0.y;
+    h.thd_off = h0.z;
+    h.thd_cnt = h0.w;
+    h.auxo = h1.x;
+    h.bint = h1.z;
+    h.fbint = h1.w;
+    const uint4 e0 = __ldg(reinterpret_cast<const uint4*>(R) + 2);
+    const uint4 e1 = __ldg(reinterpret_cast<const uint4*>(R) + 3);
+    h.ent[0] = e0.x; h.ent[1] = e0.y; h.ent[2] = e0.z; h.ent[3] = e0.w;
+    h.ent[4] = e1.x; h.ent[5] = e1.y; h.ent[6] = e1.z; h.ent[7] = e1.w;
+    h.p = R->p;
+}
+
+struct RxnTerms {
+    double net;              // pressure-modified net rate of progress
+    double g[PJG_MAXSP];     // d (rf - rr) / d c_j for participant j
+    double gns;              // the same for the bath gas (0 if absent)
+    double ci_;              // pressure modification (1 without third body)
+    double d0, d1;           // temperature and extra-variable column terms
+    double X;                // third-body column factor, Rnet d ci / d [M]
+};
+
+struct FallState {
+    double Pr, Fi, A, B, Fc, lnFc, X, lnQ, kratio;
+    double e1, e2, e3;  // Troe exponentials at the clamped temperature
+};
+
+template <bool DER, class ARR>
+__device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
+                                          const int* thd_spec, const double* thd_coef, int last,
+                                          const StateVars& sv, const ARR& conc, const ARR& bk,
+                                          const ARR& db, RxnTerms& o)
+{
+    const int flags = h.flags, nsp = h.nsp;
+    const double* p = h.p;
+    const int form = RX_FORM(flags);
+    const bool rev = flags & RX_REV;
+    const double Tc = sv.Tc, logT = sv.logT, Tinv = sv.Tinv, Tjinv = sv.Tjinv;
+
+    // forward rate constant and its log-derivatives
+    double kf, dlnkf_dT = 0.0, dlnkf_dlnP = 0.0;
+    if (form <= FORM_ARR) {
+        kf = arrhenius(form, ldg(p + P_A), ldg(p + P_B), ldg(p + P_TA), h.bint, Tc, logT, Tinv);
+        if (DER) dlnkf_dT = (ldg(p + P_B) + ldg(p + P_TA) * Tjinv) * Tjinv;
+    } else if (form == FORM_PLOG) {
+        kf = gexp(plog_logk(aux + h.auxo, logT, Tinv, sv.logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP));
+    } else {
+        const double l10 = cheb_log10k(aux + h.auxo, Tinv, sv.logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP);
+        kf = exp(LN10 * fmin(EXP_MAX, l10));
+        dlnkf_dT *= LN10;
+        dlnkf_dlnP *= LN10;
+    }
+    // reverse rate: kr = kf / Kc, Kc = (P_atm/R)^nu_sum exp(sum nu b)
+    double kr = 0.0, dB = 0.0;
+    if (rev) {
+        double Bsum = 0.0;
+#pragma unroll
+        for (int e = 0; e < PJG_MAXSP; ++e) {
+            if (e >= nsp) break;
+            const int nu = ent_nur(h.ent[e]) - ent_nuf(h.ent[e]);
+            if (nu != 0) {
+                Bsum = addnu(Bsum, nu, bk[ent_spec(h.ent[e])]);
+                if (DER) dB = addnu(dB, nu, db[ent_spec(h.ent[e])]);
+            }
+        }
+        kr = kf * ldg(p + P_PSUM) * exp(-fmin(EXP_MAX, Bsum));
+    }
+    // rates of progress (mass action on raw concentrations)
+    double rf = kf, rr = kr;
+#pragma unroll
+    for (int e = 0; e < PJG_MAXSP; ++e) {
+        if (e >= nsp) break;
+        const double c = conc[ent_spec(h.ent[e])];
+        rf = mulpow(rf, c, ent_nuf(h.ent[e]));
+        if (rev) rr = mulpow(rr, c, ent_nur(h.ent[e]));
+    }
+    // third-body / fall-off pressure modification
+    const int thd = RX_THD(flags);
+    const int blend = RX_BLEND(flags);
+    const bool chem = flags & RX_CHEM;
+    double ci = 1.0, M = 0.0;
+    FallState fs;
+    fs.Pr = 0.0; fs.Fi = 1.0; fs.A = 0.0; fs.B = 0.0; fs.Fc = 1.0; fs.lnFc = 0.0; fs.X = 0.0;
+    fs.lnQ = 0.0; fs.kratio = 0.0; fs.e1 = 0.0; fs.e2 = 0.0; fs.e3 = 0.0;
+    if (thd) {
+        M = sv.PoRT * ldg(p + P_FLAG);
+        for (int l = 0; l < h.thd_cnt; ++l)
+            M = fma(__ldg(thd_coef + h.thd_off + l), conc[__ldg(thd_spec + h.thd_off + l)], M);
+        if (blend == BL_NONE) {
+            ci = M;
+        } else {
+            const double kfall = arrhenius(RX_FFORM(flags), ldg(p + P_FA), ldg(p + P_FB),
+                                           ldg(p + P_FTA), h.fbint, Tc, logT, Tinv);
+            fs.kratio = chem ? kf / kfall : kfall / kf;  // k0 / kinf
+            fs.Pr = M * fs.kratio;
+            if (blend == BL_TROE) {
+                const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
+                const double ta = ldg(p + P_F0);
+                fs.e1 = gexp(-1.0 * Tc * ldg(p + P_F1));
+                fs.e3 = gexp(-1.0 * Tc * ldg(p + P_F3));
+                double Fc = ta * fs.e1 + (1.0 + -1.0 * ta) * fs.e3;
+                if (flags & RX_T2) {
+                    fs.e2 = gexp(-1.0 * ldg(p + P_F2) * Tinv);
+                    Fc = Fc + fs.e2;
+                }
+                fs.lnFc = log(fmax(SMALL, Fc));
+                const double logFc = fs.lnFc * INV_LN10;
+                fs.B = -1.1762 * logFc + -0.14 * logPr + 0.806;
+                fs.A = -0.67 * logFc + logPr + -0.4;
+                fs.Fc = Fc;
+                const double B2 = fs.B * fs.B;
+                fs.Fi = exp(B2 / (fs.A * fs.A + B2) * fs.lnFc);
+            } else if (blend == BL_SRI) {
+                const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
+                fs.X = 1.0 / (logPr * logPr + 1.0);
+                fs.e1 = gexp(-ldg(p + P_F1) * Tinv);
+                fs.e3 = gexp(-Tc / ldg(p + P_F2));
+                const double Q = ldg(p + P_F0) * fs.e1 + fs.e3;
+                fs.lnQ = log(Q);
+                double Fi = exp(fs.X * fs.lnQ);
+                if (flags & RX_SRID) Fi = Fi * ldg(p + P_F3);
+                if (flags & RX_SRIE) {
+                    const double e = ldg(p + P_F4);
+                    const int ie = (int)e;
+                    Fi = Fi * ((flags & RX_SRIEINT) ? (ie < 0 ? powi(Tinv, -ie) : powi(Tc, ie))
+                                                    : pow(Tc, e));
+                }
+                fs.Fi = Fi;
+            }
+            ci = fs.Fi / (1.0 + fs.Pr);
+            if (!chem) ci = ci * fs.Pr;
+        }
+    }
+    double Rnet = rf;
+    if (rev) Rnet = Rnet + -1.0 * rr;
+    o.net = thd ? Rnet * ci : Rnet;
+    if (!DER) return;
+
+    const double T = sv.T, V = sv.V, P = sv.P, PoRT = sv.PoRT, rt_inv = sv.rt_inv;
+    const bool conp = sv.conp;
+    const double kr_ = rev ? kr : 0.0;
+    double cg[PJG_MAXSP];
+#pragma unroll
+    for (int e = 0; e < PJG_MAXSP; ++e) cg[e] = e < nsp ? gsmall(conc[ent_spec(h.ent[e])]) : 1.0;
+    // d R / d c_j for every participant j (dRopidnj :4169-4522)
+    double gns = 0.0;
+#pragma unroll
+    for (int j = 0; j < PJG_MAXSP; ++j) {
+        if (j >= nsp) break;
+        const int nfj = ent_nuf(h.ent[j]), nrj = ent_nur(h.ent[j]);
+        double gf = 0.0, gr = 0.0;
+        if (nfj) {
+            double S = nux(nfj, kf);
+#pragma unroll
+            for (int e = 0; e < PJG_MAXSP; ++e) {
+                if (e >= nsp) break;
+                S = mulpow(S, cg[e], ent_nuf(h.ent[e]) - (e == j));
+            }
+            gf = S;
+        }
+        if (rev && nrj) {
+            double S = nux(nrj, kr_);
+#pragma unroll
+            for (int e = 0; e < PJG_MAXSP; ++e) {
+                if (e >= nsp) break;
+                S = mulpow(S, cg[e], ent_nur(h.ent[e]) - (e == j));
+            }
+            gr = S;
+        }
+        o.g[j] = gf - gr;
+        if (ent_spec(h.ent[j]) == last) gns = o.g[j];
+    }
+    o.gns = gns;
+    const double ci_ = thd ? ci : 1.0;
+    o.ci_ = ci_;
+    // fall-off derivative pieces shared by the n, T and E columns
+    double inv1 = 0.0, dlnFi_dPr = 0.0;
+    if (thd && blend != BL_NONE) {
+        inv1 = 1.0 / (fs.Pr + 1.0);
+        if (blend == BL_TROE) {
+            const double absq = fs.A * fs.A + fs.B * fs.B;
+            dlnFi_dPr = -2.0 * fs.A * fs.B * fs.lnFc * (0.14 * fs.A + fs.B) /
+                        (fmax(SMALL, fs.Pr) * absq * absq * LN10);
+        } else if (blend == BL_SRI) {
+            const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
+            dlnFi_dPr = -2.0 * fs.X * fs.X * logPr / (fmax(SMALL, fs.Pr) * LN10) * fs.lnQ;
+        }
+    }
+    // d ci / dx given d Pr / dx = Pr theta + theta_n and the direct part of d ln Fi / dx
+    auto dci = [&](double theta, double theta_n, double direct) -> double {
+        const double dPr = fs.Pr * theta + theta_n;
+        double d = ci * (dlnFi_dPr * dPr + direct - dPr * inv1);
+        if (!chem) d = d + theta * ci + fs.Fi * theta_n * inv1;
+        return d;
+    };
+    const double dMfac = (thd && blend != BL_NONE) ? dci(0.0, fs.kratio, 0.0) : 1.0;
+    o.X = Rnet * dMfac;
+    const double mod = ldg(p + P_MOD);
+    const bool hasns = flags & RX_HASNS;
+    // temperature column (dRopi_dT :2589-3108, dci_*_dT :2117-2588)
+    double d0 = rf * dlnkf_dT;
+    if (rev) d0 = d0 + -1.0 * rr * (dlnkf_dT + -1.0 * dB);
+    d0 = d0 * ci_ * V;
+    if (hasns) d0 += -gns * V * ci_ * PoRT * Tjinv;
+    // extra-variable column (dRopi_dE :1458-1594, dci_*_dE :362-880)
+    double d1 = 0.0;
+    if (conp) {
+        int nuf = -1, nur = -1;
+#pragma unroll
+        for (int e = 0; e < PJG_MAXSP; ++e) {
+            if (e >= nsp) break;
+            nuf += ent_nuf(h.ent[e]);
+            nur += ent_nur(h.ent[e]);
+        }
+        d1 = (-nux(nuf, rf) + (rev ? nux(nur, rr) : 0.0)) * ci_;
+    } else if (form >= FORM_PLOG) {
+        d1 = V * ci_ * Rnet * dlnkf_dlnP / P;
+    }
+    if (hasns) d1 += gns * ci_ * (conp ? PoRT : V * rt_inv);
+    if (thd) {
+        const double dM = -1.0 * PoRT * mod * Tjinv;
+        if (blend == BL_NONE) {
+            d0 += dM * V * Rnet;
+            if (conp) {
+                if (thd != THD_UNITY) d1 += (mod * PoRT + -1.0 * M) * Rnet;
+            } else {
+                d1 += V * Rnet * mod * rt_inv;
+            }
+        } else {
+            double b0, binf, Ta0, Tainf;
+            if (!chem) {
+                binf = ldg(p + P_B); Tainf = ldg(p + P_TA);
+                b0 = ldg(p + P_FB); Ta0 = ldg(p + P_FTA);
+            } else {
+                b0 = ldg(p + P_B); Ta0 = ldg(p + P_TA);
+                binf = ldg(p + P_FB); Tainf = ldg(p + P_FTA);
+            }
+            const double theta = Tjinv * (b0 + -1.0 * binf + (Ta0 + -1.0 * Tainf) * Tjinv);
+            const double theta_n = dM * fs.kratio;
+            double direct = 0.0;
+            if (blend == BL_TROE) {
+                const double absq = fs.A * fs.A + fs.B * fs.B;
+                const double ta = ldg(p + P_F0), t1 = ldg(p + P_F1), t2 = ldg(p + P_F2),
+                             t3 = ldg(p + P_F3);
+                // the explicit T derivative uses the unclamped T, as the reference
+                const bool same = T == Tc;
+                const double x1 = same ? fs.e1 : gexp(-1.0 * T * t1);
+                const double x3 = same ? fs.e3 : gexp(-1.0 * T * t3);
+                double dFc = -1.0 * ta * t1 * x1 + (ta + -1.0) * t3 * x3;
+                if (flags & RX_T2)
+                    dFc += t2 * Tjinv * Tjinv * (same ? fs.e2 : gexp(-1.0 * t2 * Tjinv));
+                direct = -fs.B * dFc *
+                         (2.0 * fs.A * (1.1762 * fs.A + -0.67 * fs.B) * fs.lnFc - fs.B * absq * LN10) /
+                         (fs.Fc * absq * absq * LN10);
+            } else if (blend == BL_SRI) {
+                const double sa = ldg(p + P_F0), sb = ldg(p + P_F1), sc = ldg(p + P_F2);
+                const double Q = sa * fs.e1 + fs.e3;
+                const double dQ = sa * sb * Tjinv * Tjinv * fs.e1 - fs.e3 / sc;
+                direct = fs.X * dQ / Q + ldg(p + P_F4) * Tjinv;
+            }
+            d0 += dci(theta, theta_n, direct) * V * Rnet;
+            const double modp = (conp ? (thd == THD_UNITY ? 0.0 : mod) * PoRT : mod * rt_inv) * fs.kratio;
+            const double th = conp ? -1.0 * (thd != THD_UNITY) : 0.0;
+            d1 += dci(th, modp, 0.0) * (conp ? 1.0 : V) * Rnet;
+        }
+    }
+    o.d0 = d0;
+    o.d1 = d1;
+}
+
+}  // namespace pjg

@@ -112,6 +112,20 @@ def test_jacobian(cuda_device, name, conp, order, fmt):
     assert row_rel_err(J, Jref) < RTOL_JAC
 
 
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_jacobian_repeats_bitwise(cuda_device, order):
+    """Each state's entries are summed by one thread in a fixed order (global
+    reductions included), so repeated calls are bitwise equal."""
+    n = 1000
+    P, phi = states("gri30", n, 14, True)
+    ev = evaluator("gri30")
+    x = phi if order == "C" else phi.T
+    tP, tx = to_dev(P, cuda_device), to_dev(x, cuda_device)
+    a = ev.jacobian(tP, tx, order=order).cpu().numpy()
+    for _ in range(3):
+        assert np.array_equal(a, ev.jacobian(tP, tx, order=order).cpu().numpy())
+
+
 def test_pywrap_kernels_match_device_api(cuda_device):
     """PyJacobianKernel / PySpecies_RatesKernel (host arrays) equal the device path."""
     mech = load_mech("gri30")
