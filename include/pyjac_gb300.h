@@ -163,6 +163,11 @@ int pjg_launch_count(int64_t* count);
 int pjg_fp64_peak(double* tflops);
 int pjg_profile_begin(void);
 int pjg_profile_end(int64_t* launches, double* total_ms);
+/* y = exp(x) through the table-driven exponential the evaluation kernels use
+ * for rate constants, equilibrium constants and fall-off blending (device
+ * pointers, asynchronous on `stream`); exposed so that its error against the
+ * CUDA library exp can be measured.  No reference counterpart. */
+int pjg_math_exp(const double* x, double* y, int64_t n, void* stream);
 
 #ifdef __cplusplus
 }

@@ -57,6 +57,7 @@ SIGNATURES = [
     ("pjg_profile_begin", ctypes.c_int, []),
     ("pjg_profile_end", ctypes.c_int, [ctypes.POINTER(ctypes.c_int64),
                                        ctypes.POINTER(ctypes.c_double)]),
+    ("pjg_math_exp", ctypes.c_int, [_VP, _VP, ctypes.c_int64, _VP]),
 ]
 
 

@@ -428,6 +428,16 @@ int pjg_fp64_peak(double* tflops)
     return 0;
 }
 
+int pjg_math_exp(const double* x, double* y, int64_t n, void* stream)
+{
+    if (n < 0) return fail(PJG_ERR_ARG, "negative size");
+    if (n == 0) return 0;
+    if (!x || !y) return fail(PJG_ERR_ARG, "null array");
+    if (pjg_launch_fexp(x, y, n, stream)) return fail(PJG_ERR_CUDA, "exp launch failed");
+    g_launches.fetch_add(1);
+    return 0;
+}
+
 int pjg_launch_count(int64_t* count)
 {
     if (!count) return fail(PJG_ERR_ARG, "null argument");

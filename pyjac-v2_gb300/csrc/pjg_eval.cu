@@ -59,6 +59,9 @@ template <int KIND>  // 0 species rates, 1 Jacobian, 2 J^T v
 __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND == 2 ? 3 : 4))
     eval_kernel(const EvalArgs a)
 {
+    __shared__ double etab[PJG_EXP_TAB];
+    fill_exp_table(etab);
+    __syncthreads();
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= a.n) return;  // no block-wide synchronisation below
     constexpr bool JAC = KIND == 1;
@@ -82,6 +85,15 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         dcpa = arr(ARR_DCP);
         ha = arr(ARR_H);
     }
+    // Per-state arrays in global scratch accumulate with fire-and-forget
+    // reductions (as the Jacobian does) and are read back from L2 after a
+    // fence; in shared memory they are plain read-modify-writes.
+    const bool gl = !a.use_smem;
+    auto accum = [&](const SV& v, int k, double x) {
+        if (gl) atomicAdd(&v[k], x);
+        else v[k] += x;
+    };
+    auto rd = [&](const SV& v, int k) -> double { return gl ? __ldcg(&v[k]) : v[k]; };
     const bool conp = a.conp;
     const double* ph = a.phi + s * a.phi_ss;
     const double T = ph[0];
@@ -99,6 +111,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     StateVars sv;
     sv.T = T; sv.Tc = Tc; sv.logT = logT; sv.Tinv = Tinv; sv.Tjinv = Tjinv;
     sv.V = V; sv.P = P; sv.PoRT = PoRT; sv.rt_inv = rt_inv; sv.logP = logP; sv.conp = conp;
+    sv.etab = etab;
 
     // concentrations (rate_subs.py get_concentrations :597-706)
     double nsum = 0.0;
@@ -167,7 +180,14 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         const int flags = h.flags, nsp = h.nsp, thd_off = h.thd_off, thd_cnt = h.thd_cnt;
         const unsigned* ent = h.ent;
         const double* p = h.p;
-        {
+        if (gl) {
+#pragma unroll
+            for (int e = 0; e < PJG_MAXSP; ++e) {
+                if (e >= nsp) break;
+                const int nu = ent_nur(ent[e]) - ent_nuf(ent[e]);
+                if (nu != 0) accum(wdot, ent_spec(ent[e]), nux(nu, o.net));
+            }
+        } else {
             // participants are distinct species: load all, then update
             double wv[PJG_MAXSP];
 #pragma unroll
@@ -201,21 +221,17 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
             }
             if (w != 0.0) {
                 const double wc = w * ci_;
-                double vo[PJG_MAXSP];
-#pragma unroll
-                for (int jb = 0; jb < PJG_MAXSP; ++jb)
-                    if (jb < nsp && ent_spec(ent[jb]) != last) vo[jb] = nsrow[ent_spec(ent[jb])];
 #pragma unroll
                 for (int jb = 0; jb < PJG_MAXSP; ++jb) {
                     if (jb >= nsp) break;
-                    if (ent_spec(ent[jb]) != last) nsrow[ent_spec(ent[jb])] = fma(wc, g[jb], vo[jb]);
+                    if (ent_spec(ent[jb]) != last) accum(nsrow, ent_spec(ent[jb]), wc * g[jb]);
                 }
                 if (hasns) vNS = fma(wc, gns, vNS);
                 if (thd) {
                     const double wx = w * X;
                     for (int l = 0; l < thd_cnt; ++l) {
                         const int j = __ldg(a.thd_spec + thd_off + l);
-                        if (j != last) nsrow[j] = fma(__ldg(a.thd_coef + thd_off + l), wx, nsrow[j]);
+                        if (j != last) accum(nsrow, j, __ldg(a.thd_coef + thd_off + l) * wx);
                     }
                     if (nslist) vNS = fma(cns, wx, vNS);
                 }
@@ -224,6 +240,11 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
             }
             continue;
         }
+        // d R / d c_j times the pressure modification, once per reaction (ci is
+        // exactly 1 without a third body)
+        double gci[PJG_MAXSP];
+#pragma unroll
+        for (int e = 0; e < PJG_MAXSP; ++e) gci[e] = e < nsp ? (thd ? g[e] * ci_ : g[e]) : 0.0;
         // scatter into the species rows of this reaction
 #pragma unroll
         for (int ka = 0; ka < PJG_MAXSP; ++ka) {
@@ -242,7 +263,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
                 if (jb >= nsp + 2) break;
                 const int sl = jb < nsp ? __ldg(slots + ka * nsp + jb)
                                         : __ldg(slots + nsp * nsp + 2 * ka + (jb - nsp));
-                const double v = jb < nsp ? g[jb] * ci_ : (jb == nsp ? d0 : d1);
+                const double v = jb < nsp ? gci[jb] : (jb == nsp ? d0 : d1);
                 if (sl >= 0) atomicAdd(accs + (int64_t)sl * a.acc_ld, nux(nuk, v));
             }
             double nsacc = 0.0;
@@ -256,30 +277,32 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
                 }
                 if (nslist) nsacc = fma(cns, X, nsacc);
             }
-            if (hasns || (thd && nslist)) nsrow[k] = addnu(nsrow[k], nuk, nsacc);
+            if (hasns || (thd && nslist)) accum(nsrow, k, nux(nuk, nsacc));
         }
     }
+
+    if (gl) __threadfence();
 
     // ------------------------------------------- temperature and E rates
     double upper = 0.0, lower = 0.0;
     if (DER) {
         for (int k = 0; k < last; ++k) {
             lower = fma(conc[k], cpa[k], lower);
-            upper = fma(ha[k], wdot[k], upper);
+            upper = fma(ha[k], rd(wdot, k), upper);
         }
         lower = fma(conc[last], cp_ns, lower);
-        upper = fma(h_ns, wdot[last], upper);
+        upper = fma(h_ns, rd(wdot, last), upper);
     } else {
         for (int k = 0; k < ns; ++k) {
             const Thermo t = thermo<false>(a.sp + (int64_t)k * PJG_SP_DOUBLES, Tc, logT, Tinv, conp);
             lower = fma(conc[k], t.cp, lower);
-            upper = fma(t.h, wdot[k], upper);
+            upper = fma(t.h, rd(wdot, k), upper);
         }
     }
     const double Tdot = 0.0 + -1.0 * upper / lower;
     double dE = 0.0;
     for (int k = 0; k < last; ++k)
-        dE = fma(ldg(a.sp + (int64_t)k * PJG_SP_DOUBLES + SP_OMW), wdot[k], dE);
+        dE = fma(ldg(a.sp + (int64_t)k * PJG_SP_DOUBLES + SP_OMW), rd(wdot, k), dE);
     const double Vval = fmax(1e-30, V);
     double Edot;
     if (conp) {
@@ -293,7 +316,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         double* o = a.dphi + s * a.dphi_ss;
         o[0] = Tdot;
         o[a.dphi_sj] = Edot;
-        for (int k = 0; k < last; ++k) o[(int64_t)(2 + k) * a.dphi_sj] = Vval * wdot[k];
+        for (int k = 0; k < last; ++k) o[(int64_t)(2 + k) * a.dphi_sj] = Vval * rd(wdot, k);
     }
     if (VJP) {
         // constant parts of columns T and E (from rows T, E of dTdot_dT :1847,
@@ -305,7 +328,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         for (int k = 0; k < last; ++k) {
             const double* rec = a.sp + (int64_t)k * PJG_SP_DOUBLES;
             const double mw = ldg(rec + SP_MW), omw = ldg(rec + SP_OMW);
-            const double wk = wdot[k], ck = conc[k], cpk = cpa[k];
+            const double wk = rd(wdot, k), ck = conc[k], cpk = cpa[k];
             dTsum = dTsum + (cp_ns * Tjinv - dcpa[k]) * ck;
             wsum = wsum + wk * (-cpk + mw * cp_ns);
             omws = fma(omw, wk, omws);
@@ -323,7 +346,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         o[0] = vout0 + C0;
         o[a.phi_sj] = vout1 + C1;
         for (int j = 0; j < last; ++j)
-            o[(int64_t)(2 + j) * a.phi_sj] = nsrow[j] - vNS + gam * (cpa[j] - cp_ns);
+            o[(int64_t)(2 + j) * a.phi_sj] = rd(nsrow, j) - vNS + gam * (cpa[j] - cp_ns);
         return;
     }
     if (!JAC) return;
@@ -336,7 +359,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     auto accr = [&](int64_t sl) { return __ldcg(acc + sl * ld); };
     // bath-gas terms: subtract the per-row sums from every species column
     for (int k = 0; k < last; ++k) {
-        const double v = nsrow[k];
+        const double v = rd(nsrow, k);
         if (v == 0.0) continue;
         const int r0 = __ldg(a.row_off + k), r1 = __ldg(a.row_off + k + 1);
         for (int q = r0; q < r1; ++q) {
@@ -371,7 +394,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         const int sl0 = __ldg(a.sp_slots + 2 * k), sl1 = __ldg(a.sp_slots + 2 * k + 1);
         const double Jk0 = sl0 >= 0 ? accr(sl0) : 0.0;
         const double Jk1 = sl1 >= 0 ? accr(sl1) : 0.0;
-        const double wk = wdot[k], ck = conc[k], cpk = cpa[k], hwk = hw[k];
+        const double wk = rd(wdot, k), ck = conc[k], cpk = cpa[k], hwk = hw[k];
         rate_sum = rate_sum + Vjinv * Jk0 * (-1.0 * hwk);
         rate_sum = rate_sum + wk * (-cpk + mw * cp_ns);
         dTsum = dTsum + (cp_ns * Tjinv - dcpa[k]) * ck;
@@ -412,26 +435,26 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
 
 }  // namespace
 
+namespace {
+
+template <int KIND>
+void launch(const EvalArgs& a, unsigned grid, cudaStream_t st, size_t smem_bytes)
+{
+    if (smem_bytes > 48 * 1024)
+        cudaFuncSetAttribute(eval_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_bytes);
+    eval_kernel<KIND><<<grid, PJG_BLOCK, smem_bytes, st>>>(a);
+}
+
+}  // namespace
+
 int pjg_launch_eval(const EvalArgs& a, int kind, void* stream, size_t smem_bytes)
 {
     if (a.n <= 0) return 0;
     cudaStream_t st = (cudaStream_t)stream;
     const unsigned grid = (unsigned)((a.n + PJG_BLOCK - 1) / PJG_BLOCK);
-    if (kind == 1) {
-        if (smem_bytes > 48 * 1024)
-            cudaFuncSetAttribute(eval_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem_bytes);
-        eval_kernel<1><<<grid, PJG_BLOCK, smem_bytes, st>>>(a);
-    } else if (kind == 2) {
-        if (smem_bytes > 48 * 1024)
-            cudaFuncSetAttribute(eval_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem_bytes);
-        eval_kernel<2><<<grid, PJG_BLOCK, smem_bytes, st>>>(a);
-    } else {
-        if (smem_bytes > 48 * 1024)
-            cudaFuncSetAttribute(eval_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem_bytes);
-        eval_kernel<0><<<grid, PJG_BLOCK, smem_bytes, st>>>(a);
-    }
+    if (kind == 1) launch<1>(a, grid, st, smem_bytes);
+    else if (kind == 2) launch<2>(a, grid, st, smem_bytes);
+    else launch<0>(a, grid, st, smem_bytes);
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }

@@ -43,9 +43,48 @@ __device__ __forceinline__ double mulpow(double acc, double v, int p)
     return acc * powi(v, p);
 }
 
+// Table of 2^(j/64), j = 0..63, in shared memory: every kernel that calls
+// fexp fills one per block with fill_exp_table before its first use.
+#define PJG_EXP_TAB 64
+
+__device__ __forceinline__ void fill_exp_table(double* tab)
+{
+    for (int j = threadIdx.x; j < PJG_EXP_TAB; j += blockDim.x) tab[j] = exp2((double)j * (1.0 / 64));
+}
+
+// exp(x) by the table-driven method of P. T. P. Tang ("Table-driven
+// implementation of the exponential function in IEEE floating-point
+// arithmetic", ACM TOMS 15(2), 1989): x = (64 m + j) ln2/64 + r with
+// |r| <= ln2/128, so exp(x) = 2^m 2^(j/64) exp(r), and exp(r) - 1 is its
+// degree-5 Taylor polynomial (truncation below 4e-17 relative).  Ten FP64
+// instructions; the scale 2^m goes into the exponent field with an integer
+// add.  |x| >= 708, infinities and NaN take the library exp.  Error about
+// 1 ulp (checked against exp in the tests).
+__device__ __forceinline__ double fexp(double x, const double* tab)
+{
+    if ((__double_as_longlong(x) & 0x7fffffffffffffffLL) >= 0x4086200000000000LL)  // |x| >= 708
+        return exp(x);
+    const double inv = 92.33248261689366;          // 64 / ln 2
+    const double l1 = 0.010830424696249145;        // ln 2 / 64, leading part
+    const double l2 = 3.623510646634843e-19;       // ln 2 / 64 - l1
+    const double shift = 6755399441055744.0;       // 1.5 * 2^52: rounds to an integer
+    const double t = fma(x, inv, shift);
+    const double nd = t - shift;                   // nearest integer to 64 x / ln 2
+    const int n = __double2loint(t);               // the same integer
+    double r = fma(-nd, l1, x);
+    r = fma(-nd, l2, r);
+    double q = fma(r, 1.0 / 120, 1.0 / 24);
+    q = fma(q, r, 1.0 / 6);
+    q = fma(q, r, 0.5);
+    q = fma(q, r, 1.0);
+    const double tj = tab[n & (PJG_EXP_TAB - 1)];
+    const double y = fma(tj, r * q, tj);
+    return __longlong_as_double(__double_as_longlong(y) + ((long long)(n >> 6) << 52));
+}
+
 // exp(min(x, 690.775527898)), the reference's guarded exponential
 // (pyjac/core/instruction_creator.py GuardedExp :436-448)
-__device__ __forceinline__ double gexp(double x) { return exp(fmin(EXP_MAX, x)); }
+__device__ __forceinline__ double gexp(double x, const double* tab) { return fexp(fmin(EXP_MAX, x), tab); }
 
 // positive-argument max(1e-300, x) guard without an FP64 instruction: for
 // x >= 0 the IEEE order equals the integer order of the bit patterns, and a
@@ -59,12 +98,12 @@ __device__ __forceinline__ double gsmall(double x)
 
 // Arrhenius forms of rate_subs.py get_simple_arrhenius_rates (:2642-3023)
 __device__ __forceinline__ double arrhenius(int form, double A, double b, double Ta, int bint,
-                                            double Tc, double logT, double Tinv)
+                                            double Tc, double logT, double Tinv, const double* tab)
 {
     if (form == FORM_A) return A;
     // fast_powi of a negative exponent inverts its base first
     if (form == FORM_AT) return A * (bint < 0 ? powi(Tinv, -bint) : powi(Tc, bint));
-    return gexp(A + logT * b + -1.0 * Ta * Tinv);
+    return gexp(A + logT * b + -1.0 * Ta * Tinv, tab);
 }
 
 // PLOG: ln kf interpolated linearly in ln P between bracketing pressures,

@@ -60,6 +60,7 @@ struct StateVars {
     double rt_inv;  // 1 / (R T)
     double logP;    // ln P (PLOG / Chebyshev mechanisms only)
     bool conp;
+    const double* etab;  // fexp table (shared memory)
 };
 
 // decoded reaction header
@@ -89,7 +90,7 @@ __device__ __forceinline__ void load_head(const PjgRxn* R, RxnHead& h)
 
 struct RxnTerms {
     double net;              // pressure-modified net rate of progress
-    double g[PJG_MAXSP];     // d (rf - rr) / d c_j for participant j
+    double g[PJG_MAXSP];          // d (rf - rr) / d c_j for participant j
     double gns;              // the same for the bath gas (0 if absent)
     double ci_;              // pressure modification (1 without third body)
     double d0, d1;           // temperature and extra-variable column terms
@@ -112,17 +113,18 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
     const int form = RX_FORM(flags);
     const bool rev = flags & RX_REV;
     const double Tc = sv.Tc, logT = sv.logT, Tinv = sv.Tinv, Tjinv = sv.Tjinv;
+    const double* et = sv.etab;
 
     // forward rate constant and its log-derivatives
     double kf, dlnkf_dT = 0.0, dlnkf_dlnP = 0.0;
     if (form <= FORM_ARR) {
-        kf = arrhenius(form, ldg(p + P_A), ldg(p + P_B), ldg(p + P_TA), h.bint, Tc, logT, Tinv);
+        kf = arrhenius(form, ldg(p + P_A), ldg(p + P_B), ldg(p + P_TA), h.bint, Tc, logT, Tinv, et);
         if (DER) dlnkf_dT = (ldg(p + P_B) + ldg(p + P_TA) * Tjinv) * Tjinv;
     } else if (form == FORM_PLOG) {
-        kf = gexp(plog_logk(aux + h.auxo, logT, Tinv, sv.logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP));
+        kf = gexp(plog_logk(aux + h.auxo, logT, Tinv, sv.logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP), et);
     } else {
         const double l10 = cheb_log10k(aux + h.auxo, Tinv, sv.logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP);
-        kf = exp(LN10 * fmin(EXP_MAX, l10));
+        kf = fexp(LN10 * fmin(EXP_MAX, l10), et);
         dlnkf_dT *= LN10;
         dlnkf_dlnP *= LN10;
     }
@@ -139,7 +141,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                 if (DER) dB = addnu(dB, nu, db[ent_spec(h.ent[e])]);
             }
         }
-        kr = kf * ldg(p + P_PSUM) * exp(-fmin(EXP_MAX, Bsum));
+        kr = kf * ldg(p + P_PSUM) * fexp(-fmin(EXP_MAX, Bsum), et);
     }
     // rates of progress (mass action on raw concentrations)
     double rf = kf, rr = kr;
@@ -166,17 +168,17 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
             ci = M;
         } else {
             const double kfall = arrhenius(RX_FFORM(flags), ldg(p + P_FA), ldg(p + P_FB),
-                                           ldg(p + P_FTA), h.fbint, Tc, logT, Tinv);
+                                           ldg(p + P_FTA), h.fbint, Tc, logT, Tinv, et);
             fs.kratio = chem ? kf / kfall : kfall / kf;  // k0 / kinf
             fs.Pr = M * fs.kratio;
             if (blend == BL_TROE) {
                 const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
                 const double ta = ldg(p + P_F0);
-                fs.e1 = gexp(-1.0 * Tc * ldg(p + P_F1));
-                fs.e3 = gexp(-1.0 * Tc * ldg(p + P_F3));
+                fs.e1 = gexp(-1.0 * Tc * ldg(p + P_F1), et);
+                fs.e3 = gexp(-1.0 * Tc * ldg(p + P_F3), et);
                 double Fc = ta * fs.e1 + (1.0 + -1.0 * ta) * fs.e3;
                 if (flags & RX_T2) {
-                    fs.e2 = gexp(-1.0 * ldg(p + P_F2) * Tinv);
+                    fs.e2 = gexp(-1.0 * ldg(p + P_F2) * Tinv, et);
                     Fc = Fc + fs.e2;
                 }
                 fs.lnFc = log(fmax(SMALL, Fc));
@@ -185,15 +187,15 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                 fs.A = -0.67 * logFc + logPr + -0.4;
                 fs.Fc = Fc;
                 const double B2 = fs.B * fs.B;
-                fs.Fi = exp(B2 / (fs.A * fs.A + B2) * fs.lnFc);
+                fs.Fi = fexp(B2 / (fs.A * fs.A + B2) * fs.lnFc, et);
             } else if (blend == BL_SRI) {
                 const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
                 fs.X = 1.0 / (logPr * logPr + 1.0);
-                fs.e1 = gexp(-ldg(p + P_F1) * Tinv);
-                fs.e3 = gexp(-Tc / ldg(p + P_F2));
+                fs.e1 = gexp(-ldg(p + P_F1) * Tinv, et);
+                fs.e3 = gexp(-Tc / ldg(p + P_F2), et);
                 const double Q = ldg(p + P_F0) * fs.e1 + fs.e3;
                 fs.lnQ = log(Q);
-                double Fi = exp(fs.X * fs.lnQ);
+                double Fi = fexp(fs.X * fs.lnQ, et);
                 if (flags & RX_SRID) Fi = Fi * ldg(p + P_F3);
                 if (flags & RX_SRIE) {
                     const double e = ldg(p + P_F4);
@@ -320,11 +322,11 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                              t3 = ldg(p + P_F3);
                 // the explicit T derivative uses the unclamped T, as the reference
                 const bool same = T == Tc;
-                const double x1 = same ? fs.e1 : gexp(-1.0 * T * t1);
-                const double x3 = same ? fs.e3 : gexp(-1.0 * T * t3);
+                const double x1 = same ? fs.e1 : gexp(-1.0 * T * t1, et);
+                const double x3 = same ? fs.e3 : gexp(-1.0 * T * t3, et);
                 double dFc = -1.0 * ta * t1 * x1 + (ta + -1.0) * t3 * x3;
                 if (flags & RX_T2)
-                    dFc += t2 * Tjinv * Tjinv * (same ? fs.e2 : gexp(-1.0 * t2 * Tjinv));
+                    dFc += t2 * Tjinv * Tjinv * (same ? fs.e2 : gexp(-1.0 * t2 * Tjinv, et));
                 direct = -fs.B * dFc *
                          (2.0 * fs.A * (1.1762 * fs.A + -0.67 * fs.B) * fs.lnFc - fs.B * absq * LN10) /
                          (fs.Fc * absq * absq * LN10);

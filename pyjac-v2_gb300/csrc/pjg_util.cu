@@ -2,8 +2,18 @@
 // and the FP64 throughput probe used as the FP64 roofline denominator.
 #include <cuda_runtime.h>
 #include "pjg_eval.cuh"
+#include "pjg_math.cuh"
 
 namespace {
+
+__global__ void fexp_kernel(const double* x, double* y, int64_t n)
+{
+    __shared__ double tab[PJG_EXP_TAB];
+    pjg::fill_exp_table(tab);
+    __syncthreads();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = pjg::fexp(x[i], tab);
+}
 
 __global__ void zero_acc(double* acc, int64_t ld, int64_t n, int nslot)
 {
@@ -67,5 +77,12 @@ int pjg_launch_transpose(const double* src, int64_t ld, int64_t n, int nslot, do
     if (n <= 0 || nslot <= 0) return 0;
     dim3 grid((unsigned)((n + 31) / 32), (unsigned)((nslot + 31) / 32));
     transpose_kernel<<<grid, dim3(32, 8), 0, (cudaStream_t)stream>>>(src, ld, n, nslot, dst);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int pjg_launch_fexp(const double* x, double* y, int64_t n, void* stream)
+{
+    if (n <= 0) return 0;
+    fexp_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, y, n);
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }

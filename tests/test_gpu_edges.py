@@ -120,3 +120,31 @@ def test_problem_spanning_several_launch_chunks(cuda_device, order, n):
     Jref = oracle_mod().Oracle(mech).jacobian(P[pick], phi[pick])
     assert np.isfinite(J).all()
     assert row_rel_err(J, Jref) < RTOL_JAC
+
+
+def test_table_driven_exp_against_cuda_exp(cuda_device):
+    """The kernels' exponential (Tang's table-driven method) against the CUDA
+    library exp (each within about 1 ulp of the true value): at most 3 ulp
+    apart over the range the kinetics use, identical beyond |x| = 708 where the
+    library takes over, and the same IEEE special values."""
+    import torch
+    lib = pkg("_lib")
+    rng = np.random.default_rng(17)
+    x = np.concatenate([rng.uniform(-745.0, 709.7, 2_000_000), rng.uniform(-1, 1, 500_000),
+                        rng.uniform(-1e-8, 1e-8, 100_000),
+                        np.array([0.0, -0.0, 1.0, -1.0, 707.999, -707.999, 708.0, -708.0, 709.7,
+                                  -745.0, 690.775527898, -690.775527898, 800.0, -800.0,
+                                  np.inf, -np.inf, np.nan])])
+    tx = torch.from_numpy(x).to(cuda_device)
+    y = torch.empty_like(tx)
+    st = torch.cuda.current_stream(cuda_device).cuda_stream
+    assert lib.load().pjg_math_exp(tx.data_ptr(), y.data_ptr(), tx.numel(), st) == 0
+    ref = torch.exp(tx)  # the CUDA library exp
+    torch.cuda.synchronize()
+    y, ref = y.cpu().numpy(), ref.cpu().numpy()
+    same_class = (np.isnan(y) == np.isnan(ref)) & (np.isinf(y) == np.isinf(ref))
+    assert same_class.all()
+    fin = np.isfinite(ref) & (ref > 0)
+    ulp = np.abs(y[fin] - ref[fin]) / np.spacing(ref[fin])
+    assert ulp.max() <= 3.0, ulp.max()
+    assert (y[~fin & ~np.isnan(ref)] == ref[~fin & ~np.isnan(ref)]).all()

@@ -160,3 +160,4 @@ def test_indices_bit_exact_device(cuda_device):
             ptr, ind = ev.jacobian_indices(order)
             eptr, eind = mech.pattern(order)
             assert np.array_equal(ptr, eptr) and np.array_equal(ind, eind)
+
