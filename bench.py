@@ -30,13 +30,20 @@ import importlib  # noqa: E402
 PKG = "pyjac-v2_gb300"
 METRIC = "GRI-30 FP64 Jacobians/s"
 UNIT = "Jacobians/s"
+# per --kernel: metric, unit, evaluation kernel
+KERNELS = {
+    "jacobian": (METRIC, UNIT, "eval_kernel<1> (fused Jacobian)"),
+    "rates": ("GRI-30 FP64 species-rate evaluations/s", "states/s", "eval_kernel<0> (species rates)"),
+    "vjp": ("GRI-30 FP64 J^T v products/s", "states/s", "eval_kernel<2> (J^T v)"),
+}
+# measured FP64 instruction / DRAM counts per state (ncu), see profiles/
+COUNTS = os.path.join(ROOT, "profiles", "gri30_kernel_counts.json")
 
-# algorithmic HBM bytes per state: read phi (NN) + param, write NN^2 (dense)
-NN_GRI = 54
 
-
-def alg_bytes_per_state(nn, n_out):
-    return 8 * (nn + 1) + 8 * n_out
+def alg_bytes_per_state(nn, n_out, n_in=None):
+    """Algorithmic HBM bytes per state: read phi (NN) + param (+ v for J^T v),
+    write n_out values."""
+    return 8 * (nn + 1 if n_in is None else n_in) + 8 * n_out
 
 
 def pkg(sub=None):
@@ -242,6 +249,8 @@ def main():
     ap.add_argument("--sur-train", type=int, default=1 << 22)
     ap.add_argument("--sur-epochs", type=int, default=12)
     ap.add_argument("--sur-eval", type=int, default=1 << 22)
+    ap.add_argument("--kernel", default="jacobian", choices=sorted(KERNELS),
+                    help="evaluation timed: the Jacobian (headline), species rates or J^T v")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -262,16 +271,29 @@ def main():
     ev = api.Evaluator(mech)
     n = args.states
     nn = mech.nn
-    n_out = nn * nn if args.format == "full" else mech.jac_nnz()
+    metric, unit, kname = KERNELS[args.kernel]
+    if args.kernel == "jacobian":
+        n_out = nn * nn if args.format == "full" else mech.jac_nnz()
+        n_in = nn + 1
+    else:
+        n_out = nn
+        n_in = nn + 1 if args.kernel == "rates" else 2 * nn + 1
     P, phi = states.draw_states(mech.n_species, n, seed=1000 + rank, x_floor=1e-12)
     x = np.ascontiguousarray(phi.T) if args.order == "F" else phi
     tP = torch.from_numpy(P).to(dev)
     tphi = torch.from_numpy(x).to(dev)
     out = torch.empty(n * n_out, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
+    if args.kernel == "vjp":
+        tv = torch.from_numpy(np.random.default_rng(77).standard_normal(x.shape)).to(dev)
 
     def step():
-        ev.jacobian(tP, tphi, order=args.order, conp=True, jac_format=args.format, out=out)
+        if args.kernel == "jacobian":
+            ev.jacobian(tP, tphi, order=args.order, conp=True, jac_format=args.format, out=out)
+        elif args.kernel == "rates":
+            ev.species_rates(tP, tphi, order=args.order, conp=True, out=out.view(tphi.shape))
+        else:
+            ev.vjp(tP, tphi, tv, order=args.order, conp=True, out=out.view(tphi.shape))
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -304,86 +326,89 @@ def main():
     ms_step = ms / args.steps
     value = world * n * args.steps / (ms * 1e-3)
 
-    # roofline of the dominant kernel (the fused Jacobian evaluation kernel)
-    bytes_step = alg_bytes_per_state(nn, n_out) * n
-    achieved = bytes_step * args.steps / (eval_ms * 1e-3) / 1e9
+    # roofline of the timed evaluation kernel
+    bpsi = alg_bytes_per_state(nn, n_out, n_in)
+    per_launch = n / max(1, n_eval // args.steps)  # states one launch covers
+    achieved = bpsi * n * args.steps / (eval_ms * 1e-3) / 1e9
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     hbm_peak, peak_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):
         with open(peaks_path) as fh:
             hbm_peak = float(json.load(fh).get("hbm_gbs", hbm_peak))
         peak_src = "measured"
-    flops_path = os.path.join(ROOT, "profiles", "fp64_ops_gri30_jacobian.json")
+    key = "%s_%s_%s" % (args.kernel, args.format if args.kernel == "jacobian" else "na", args.order)
+    counts = {}
+    if os.path.exists(COUNTS):
+        with open(COUNTS) as fh:
+            counts = json.load(fh).get(key, {})
+    krate = n * args.steps / (eval_ms * 1e-3)  # states/s of the evaluation kernel alone
     fp64 = {"peak": fp64_peak.value, "unit": "TFLOP/s",
             "peak_source": "measured DFMA probe (pjg_fp64_peak)"}
-    if os.path.exists(flops_path):
-        with open(flops_path) as fh:
-            fl = json.load(fh)
-        key = "%s_%s" % (args.format, args.order)
-        if key in fl.get("flops_per_state", {}):
-            fps = fl["flops_per_state"][key]
-            ach = fps * n * args.steps / (eval_ms * 1e-3) / 1e12
-            fp64 = {"achieved": ach, "peak": fp64_peak.value, "unit": "TFLOP/s",
-                    "frac": ach / fp64_peak.value, "flops_per_state": fps,
-                    "peak_source": "measured DFMA probe (pjg_fp64_peak)"}
+    if counts:
+        fl, ins = counts["fp64_flops_per_state"], counts["fp64_inst_per_state"]
+        fp64.update({"achieved": fl * krate / 1e12, "frac": fl * krate / 1e12 / fp64_peak.value,
+                     "flops_per_state": fl, "pipe_inst_per_state": ins,
+                     "pipe_frac": ins * krate / (fp64_peak.value * 1e12 / 2),
+                     "counts": "ncu, %s (profiles/)" % counts.get("case", "")})
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None,
-                "peak_source": peak_src, "kernel": "eval_kernel<1> (fused Jacobian)",
-                "alg_bytes_per_state": alg_bytes_per_state(nn, n_out),
+                "frac": achieved / hbm_peak,
+                "traffic": (counts["dram_bytes_per_state"] * per_launch
+                            if counts.get("dram_bytes_per_state") else None),
+                "peak_source": peak_src, "kernel": kname, "alg_bytes_per_state": bpsi,
                 "eval_ms_per_step": eval_ms / args.steps, "eval_launches": n_eval,
+                "binding": "fp64 pipe: see fp64.pipe_frac (FP64 instructions x rate / DFMA rate)",
                 "fp64": fp64}
-    traffic_path = os.path.join(ROOT, "profiles", "traffic_gri30_jacobian.json")
-    if os.path.exists(traffic_path):
-        with open(traffic_path) as fh:
-            tr = json.load(fh)
-        key = "%s_%s" % (args.format, args.order)
-        if key in tr.get("dram_bytes_per_state", {}):
-            roofline["traffic"] = tr["dram_bytes_per_state"][key] * n / max(1, n_eval // args.steps)
 
     # end to end through the reference-facing kernel object, host buffers (pinned)
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and args.kernel != "vjp":
         mod = api.pywrap(mech, order=args.order, conp=True, jac_format=args.format)
-        jk = mod.PyJacobianKernel(n, 1)
+        kobj = (mod.PyJacobianKernel if args.kernel == "jacobian" else mod.PySpecies_RatesKernel)(n, 1)
         hP = torch.from_numpy(P).pin_memory().numpy()
         hphi = torch.from_numpy(x).pin_memory().numpy()
-        hjac = torch.empty(n * n_out, dtype=torch.float64, pin_memory=True).numpy()
-        jk(hP, hphi, hjac)
+        hout = torch.empty(n * n_out, dtype=torch.float64, pin_memory=True).numpy()
+        kobj(hP, hphi, hout)
         k2 = max(1, min(args.steps, 3))
         if world > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
         for _ in range(k2):
-            jk(hP, hphi, hjac)
+            kobj(hP, hphi, hout)
         sec = (time.perf_counter() - t0) / k2
-        e2e = {"value": world * n / sec, "unit": UNIT,
+        e2e = {"value": world * n / sec, "unit": unit,
                "h2d_bytes_per_step": int(hP.nbytes + hphi.nbytes),
-               "d2h_bytes_per_step": int(hjac.nbytes), "steps": k2,
-               "path": "PyJacobianKernel(problem_size, work_size)(param, phi, jac), pinned host arrays"}
-        jk.close()
-        del hjac
+               "d2h_bytes_per_step": int(hout.nbytes), "steps": k2,
+               "path": "%s(problem_size, work_size)(param, phi, out), pinned host arrays"
+                       % type(kobj).__name__}
+        kobj.close()
+        del hout
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and not args.no_cpu and args.kernel == "jacobian":
         cpu, _ = cpu_reference_run(mech, args.cpu_sample, 1)
 
     sur = None
-    if not args.no_surrogate:
+    if not args.no_surrogate and args.kernel == "jacobian":
         del out
         torch.cuda.empty_cache()
         sur = surrogate_bench(mech, ev, dev, args.sur_train, args.sur_epochs, args.sur_eval,
                               log=lambda h: print(json.dumps(h), file=sys.stderr))
 
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        line = {"metric": metric, "value": value, "unit": unit, "n_gpus": world,
                 "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "GRI-Mech 3.0 %s FP64 Jacobian, %s order, %d states"
-                           % ("dense" if args.format == "full" else "sparse CCS/CRS", args.order, n),
+                "config": {"workload": ("GRI-Mech 3.0 %s FP64 Jacobian, %s order, %d states"
+                                        % ("dense" if args.format == "full" else "sparse CCS/CRS",
+                                           args.order, n)) if args.kernel == "jacobian" else
+                           ("GRI-Mech 3.0 FP64 %s, %s order, %d states"
+                            % ("species rates" if args.kernel == "rates" else "J^T v", args.order, n)),
                            "mechanism": "grimech30 (53 species, 325 reactions)",
                            "states": n, "order": args.order, "jac_format": args.format,
-                           "conp": True, "l2": "inputs 432 MB and outputs > L2; no flush"},
+                           "conp": True,
+                           "l2": "inputs %.0f MB and outputs %.0f MB, both larger than L2 (126 MB): "
+                                 "no flush" % (8e-6 * n_in * n, 8e-6 * n_out * n)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": launches, "clocks": clk, "surrogate": sur}
         print(json.dumps(line))
