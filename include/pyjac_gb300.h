@@ -89,7 +89,10 @@ int pjg_jacobian_indices(const pjg_mech* mech, char order, int32_t* ptr, int32_t
                          int32_t* nnz);
 
 /* Device-pointer entry points (asynchronous on `stream`).
- * Replace the generated species_rates / jacobian drivers. */
+ * Replace the generated species_rates / jacobian drivers.  Calls on one
+ * mechanism share its device working buffer (grown on demand): calls that
+ * can overlap on the GPU, on different streams, must be serialised by the
+ * caller or use separate pjg_mech objects. */
 int pjg_species_rates(pjg_mech* mech, int64_t n, char order, int conp, const double* param,
                       const double* phi, double* dphi, void* stream);
 int pjg_jacobian(pjg_mech* mech, int64_t n, char order, int conp, int jac_format,
@@ -115,8 +118,13 @@ int pjg_vjp_noalloc(pjg_mech* mech, int64_t n, char order, int conp, const doubl
 /* Kernel objects: the reference's Kernel class (kernel.hpp.in:86-335).
  * problem_size = states per call; work_size is accepted for API
  * compatibility (the reference's OpenMP thread / OpenCL group count) and
- * ignored: the GPU kernels size their own grids.  Host pointers; each call
- * copies inputs in, evaluates, copies outputs out and synchronises. */
+ * ignored: the GPU kernels size their own grids.  Host pointers (pinned host
+ * memory lets the copies overlap the evaluation); each call streams the
+ * states through a ring of three device buffers of two waves of resident
+ * blocks each (155,648 states on a 152-SM GB300), copying one chunk in and
+ * another out while a third is evaluated, and returns when the outputs are
+ * in `out`.  A kernel object owns its device buffers, so kernel objects may
+ * be used from different threads at once. */
 int pjg_kernel_create(pjg_mech* mech, int kind, size_t problem_size, size_t work_size,
                       char order, int conp, int jac_format, pjg_kernel** out);
 int pjg_kernel_resize(pjg_kernel* k, size_t problem_size, size_t work_size);

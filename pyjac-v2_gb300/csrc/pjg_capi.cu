@@ -90,14 +90,31 @@ struct pjg_mech {
     size_t work_bytes = 0;
 };
 
+// Kernel object (host-pointer calls).  A call streams the problem through
+// kRing device buffers: while chunk c is evaluated, chunk c+1 is copied in
+// and chunk c-1 copied out (the copy engines run beside the kernels), on
+// three streams ordered by events.  A chunk is PJG_CHUNK_WAVES full waves of
+// resident Jacobian blocks: a launch of a fraction of a wave takes as long as
+// a whole one.
+constexpr int kRing = 3;
+#ifndef PJG_CHUNK_WAVES
+#define PJG_CHUNK_WAVES 2
+#endif
+
 struct pjg_kernel {
     pjg_mech* mech = nullptr;
     int kind = 0, conp = 1, jac_format = 0;
     char order = 'C';
     size_t problem_size = 0, work_size = 0;
-    double *d_param = nullptr, *d_phi = nullptr, *d_out = nullptr;
+    int64_t chunk = 0;                 // states per device buffer
+    double* d_param[kRing] = {};
+    double* d_phi[kRing] = {};
+    double* d_out[kRing] = {};
+    double* work = nullptr;            // per-state working arrays of one chunk
+    size_t work_bytes = 0;
     size_t out_per_state = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
+    cudaEvent_t ev_in[kRing] = {}, ev_k[kRing] = {}, ev_out[kRing] = {};
 };
 
 namespace {
@@ -210,14 +227,26 @@ bool rates_fit_smem(const pjg_mech* m)
     return (size_t)ARR_N_RATES * m->ns * PJG_BLOCK * sizeof(double) <= 200 * 1024;
 }
 
-constexpr size_t kWorkBudget = size_t(1) << 30;  // bytes of working buffer per call
+constexpr size_t kWorkBudget = size_t(8) << 30;  // bytes of working buffer per call
 
-int64_t chunk_states(size_t per_state, int64_t n)
+// States one launch can take with per_state bytes of working arrays: a whole
+// number of waves of resident blocks where the budget allows (a launch of a
+// fraction of a wave takes as long as a full wave), at most n.
+int64_t chunk_states(size_t per_state, int64_t n, int64_t wave)
 {
     if (per_state == 0) return n;
     int64_t c = (int64_t)(kWorkBudget / per_state);
-    c = std::max<int64_t>(PJG_BLOCK, c / PJG_BLOCK * PJG_BLOCK);
+    if (c >= wave) c = c / wave * wave;
+    else c = std::max<int64_t>(PJG_BLOCK, c / PJG_BLOCK * PJG_BLOCK);
     return std::min<int64_t>(c, n);
+}
+
+// States of one full wave of the evaluation kernel of `kind` on the mechanism's device.
+int64_t wave_states(const pjg_mech* m, int kind, size_t smem_bytes)
+{
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
+    return (int64_t)sms * pjg_eval_blocks_per_sm(kind, smem_bytes) * PJG_BLOCK;
 }
 
 int ensure_work(pjg_mech* m, size_t bytes)
@@ -244,9 +273,21 @@ void fill_common(const pjg_mech* m, EvalArgs& a)
     a.need_logP = m->need_logP;
 }
 
+// Per-state bytes of working arrays one evaluation needs (0: shared memory only).
+// The Jacobian accumulates in scratch for order 'C' (then transposed); an
+// output of order 'F' is its own accumulator.
+size_t eval_state_bytes(const pjg_mech* m, int kind, bool F, const SlotTables* t)
+{
+    if (kind == PJG_SPECIES_RATES && rates_fit_smem(m)) return 0;
+    return state_bytes(m, kind, kind == PJG_JACOBIAN && !F, t ? t->nslot : 0);
+}
+
+// Evaluate n states.  The per-state working arrays go to ext_work (ext_bytes)
+// when given, else to the mechanism's shared buffer, grown on demand; larger
+// problems run as several launches.
 int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_format,
              const double* param, const double* phi, double* out, cudaStream_t st,
-             const double* v = nullptr)
+             const double* v = nullptr, double* ext_work = nullptr, size_t ext_bytes = 0)
 {
     if (!m) return fail(PJG_ERR_ARG, "null mechanism");
     if (n < 0) return fail(PJG_ERR_ARG, "negative problem size");
@@ -264,12 +305,20 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
         if (rc) return rc;
     }
     const bool smem = kind == PJG_SPECIES_RATES && rates_fit_smem(m);
-    size_t per_state = smem ? 0 : state_bytes(m, kind, !F, t ? t->nslot : 0);
-    if (kind == PJG_JACOBIAN && !F) per_state = state_bytes(m, kind, true, t->nslot);
-    const int64_t ch = chunk_states(per_state, n);
-    if (per_state) {
-        int rc = ensure_work(m, per_state * (size_t)ch);
-        if (rc) return rc;
+    const size_t per_state = eval_state_bytes(m, kind, F, t);
+    int64_t ch;
+    double* work = ext_work;
+    if (ext_work) {
+        ch = per_state ? (int64_t)(ext_bytes / per_state) / PJG_BLOCK * PJG_BLOCK : n;
+        if (ch < PJG_BLOCK && ch < n) return fail(PJG_ERR_ARG, "working buffer too small");
+        ch = std::min<int64_t>(std::max<int64_t>(ch, 1), n);
+    } else {
+        ch = chunk_states(per_state, n, wave_states(m, kind, 0));
+        if (per_state) {
+            int rc = ensure_work(m, per_state * (size_t)ch);
+            if (rc) return rc;
+        }
+        work = m->work;
     }
     for (int64_t off = 0; off < n; off += ch) {
         const int64_t cnt = std::min<int64_t>(ch, n - off);
@@ -288,7 +337,7 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
             a.phi_sj = 1;
         }
         a.use_smem = smem;
-        a.scratch = m->work;
+        a.scratch = work;
         a.sc_ld = ch;
         size_t smem_bytes = smem ? (size_t)ARR_N_RATES * m->ns * PJG_BLOCK * sizeof(double) : 0;
         if (kind == PJG_SPECIES_RATES) {
@@ -304,7 +353,7 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
                 a.acc = out + off;
                 a.acc_ld = n;
             } else {
-                a.acc = m->work + (size_t)ARR_N_JAC * m->ns * ch;
+                a.acc = work + (size_t)ARR_N_JAC * m->ns * ch;
                 a.acc_ld = ch;
             }
             a.rxn_slot_off = t->rxn_slot_off;
@@ -622,9 +671,16 @@ int pjg_kernel_create(pjg_mech* m, int kind, size_t problem_size, size_t work_si
     k->jac_format = jac_format;
     k->out_per_state = kind == PJG_SPECIES_RATES ? m->nn
                        : (jac_format == PJG_JAC_SPARSE ? (size_t)m->nnz : (size_t)m->nn * m->nn);
-    if (cudaStreamCreateWithFlags(&k->stream, cudaStreamNonBlocking) != cudaSuccess) {
-        delete k;
-        return fail(PJG_ERR_CUDA, "cudaStreamCreate failed");
+    bool ok = cudaStreamCreateWithFlags(&k->s_in, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&k->s_comp, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&k->s_out, cudaStreamNonBlocking) == cudaSuccess;
+    for (int b = 0; ok && b < kRing; ++b)
+        ok = cudaEventCreateWithFlags(&k->ev_in[b], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&k->ev_k[b], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&k->ev_out[b], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        pjg_kernel_destroy(k);
+        return fail(PJG_ERR_CUDA, "stream or event creation failed");
     }
     int rc = pjg_kernel_resize(k, problem_size, work_size);
     if (rc) {
@@ -635,56 +691,123 @@ int pjg_kernel_create(pjg_mech* m, int kind, size_t problem_size, size_t work_si
     return 0;
 }
 
+namespace {
+
+void free_buffers(pjg_kernel* k)
+{
+    for (int b = 0; b < kRing; ++b) {
+        cudaFree(k->d_param[b]);
+        cudaFree(k->d_phi[b]);
+        cudaFree(k->d_out[b]);
+        k->d_param[b] = k->d_phi[b] = k->d_out[b] = nullptr;
+    }
+    cudaFree(k->work);
+    k->work = nullptr;
+    k->work_bytes = 0;
+    k->chunk = 0;
+}
+
+}  // namespace
+
 int pjg_kernel_resize(pjg_kernel* k, size_t problem_size, size_t work_size)
 {
     if (!k) return fail(PJG_ERR_ARG, "null kernel");
     k->work_size = work_size;
-    if (problem_size == k->problem_size && k->d_phi) return 0;
-    cudaFree(k->d_param);
-    cudaFree(k->d_phi);
-    cudaFree(k->d_out);
-    k->d_param = k->d_phi = k->d_out = nullptr;
+    const int64_t wave = wave_states(k->mech, PJG_JACOBIAN, 0);
+    const int64_t chunk = std::min<int64_t>((int64_t)problem_size, PJG_CHUNK_WAVES * wave);
+    if (chunk == k->chunk && k->d_phi[0]) {
+        k->problem_size = problem_size;
+        return 0;
+    }
+    free_buffers(k);
     k->problem_size = problem_size;
     if (problem_size == 0) return 0;
-    const size_t nn = k->mech->nn;
-    CUDA_TRY(cudaMalloc((void**)&k->d_param, problem_size * sizeof(double)));
-    CUDA_TRY(cudaMalloc((void**)&k->d_phi, problem_size * nn * sizeof(double)));
-    CUDA_TRY(cudaMalloc((void**)&k->d_out, problem_size * k->out_per_state * sizeof(double)));
+    pjg_mech* m = k->mech;
+    SlotTables* t = nullptr;
+    if (k->kind == PJG_JACOBIAN) {
+        int rc = build_slots(m, k->order == 'F', k->jac_format == PJG_JAC_SPARSE, &t);
+        if (rc) return rc;
+    }
+    const size_t nn = m->nn;
+    for (int b = 0; b < kRing; ++b) {
+        CUDA_TRY(cudaMalloc((void**)&k->d_param[b], chunk * sizeof(double)));
+        CUDA_TRY(cudaMalloc((void**)&k->d_phi[b], chunk * nn * sizeof(double)));
+        CUDA_TRY(cudaMalloc((void**)&k->d_out[b], chunk * k->out_per_state * sizeof(double)));
+    }
+    const size_t per_state = eval_state_bytes(m, k->kind, k->order == 'F', t);
+    const int64_t padded = (chunk + PJG_BLOCK - 1) / PJG_BLOCK * PJG_BLOCK;
+    k->work_bytes = per_state * (size_t)padded;
+    if (k->work_bytes) CUDA_TRY(cudaMalloc((void**)&k->work, k->work_bytes));
+    k->chunk = chunk;
     return 0;
 }
 
 int pjg_kernel_call(pjg_kernel* k, const double* param, const double* phi, double* out)
 {
     if (!k) return fail(PJG_ERR_ARG, "null kernel");
-    const size_t n = k->problem_size, nn = k->mech->nn;
+    const int64_t n = (int64_t)k->problem_size, nn = k->mech->nn, no = (int64_t)k->out_per_state;
     if (n == 0) return 0;
     if (!param || !phi || !out) return fail(PJG_ERR_ARG, "null array");
-    CUDA_TRY(cudaMemcpyAsync(k->d_param, param, n * sizeof(double), cudaMemcpyHostToDevice, k->stream));
-    CUDA_TRY(cudaMemcpyAsync(k->d_phi, phi, n * nn * sizeof(double), cudaMemcpyHostToDevice, k->stream));
-    int rc = run_eval(k->mech, k->kind, (int64_t)n, k->order, k->conp, k->jac_format, k->d_param,
-                      k->d_phi, k->d_out, k->stream);
-    if (rc) return rc;
-    CUDA_TRY(cudaMemcpyAsync(out, k->d_out, n * k->out_per_state * sizeof(double),
-                             cudaMemcpyDeviceToHost, k->stream));
-    CUDA_TRY(cudaStreamSynchronize(k->stream));
+    const bool F = k->order == 'F';
+    const int64_t C = k->chunk;
+    for (int64_t c = 0, s0 = 0; s0 < n; ++c, s0 += C) {
+        const int b = (int)(c % kRing);
+        const int64_t cnt = std::min<int64_t>(C, n - s0);
+        if (c >= kRing) CUDA_TRY(cudaStreamWaitEvent(k->s_in, k->ev_k[b], 0));
+        CUDA_TRY(cudaMemcpyAsync(k->d_param[b], param + s0, cnt * sizeof(double),
+                                 cudaMemcpyHostToDevice, k->s_in));
+        if (F)  // field j of the chunk: cnt contiguous doubles at phi[s0 + n * j]
+            CUDA_TRY(cudaMemcpy2DAsync(k->d_phi[b], cnt * sizeof(double), phi + s0, n * sizeof(double),
+                                       cnt * sizeof(double), nn, cudaMemcpyHostToDevice, k->s_in));
+        else
+            CUDA_TRY(cudaMemcpyAsync(k->d_phi[b], phi + s0 * nn, cnt * nn * sizeof(double),
+                                     cudaMemcpyHostToDevice, k->s_in));
+        CUDA_TRY(cudaEventRecord(k->ev_in[b], k->s_in));
+        CUDA_TRY(cudaStreamWaitEvent(k->s_comp, k->ev_in[b], 0));
+        if (c >= kRing) CUDA_TRY(cudaStreamWaitEvent(k->s_comp, k->ev_out[b], 0));
+        int rc = run_eval(k->mech, k->kind, cnt, k->order, k->conp, k->jac_format, k->d_param[b],
+                          k->d_phi[b], k->d_out[b], k->s_comp, nullptr, k->work, k->work_bytes);
+        if (rc) {
+            cudaStreamSynchronize(k->s_out);
+            return rc;
+        }
+        CUDA_TRY(cudaEventRecord(k->ev_k[b], k->s_comp));
+        CUDA_TRY(cudaStreamWaitEvent(k->s_out, k->ev_k[b], 0));
+        if (F)
+            CUDA_TRY(cudaMemcpy2DAsync(out + s0, n * sizeof(double), k->d_out[b], cnt * sizeof(double),
+                                       cnt * sizeof(double), no, cudaMemcpyDeviceToHost, k->s_out));
+        else
+            CUDA_TRY(cudaMemcpyAsync(out + s0 * no, k->d_out[b], cnt * no * sizeof(double),
+                                     cudaMemcpyDeviceToHost, k->s_out));
+        CUDA_TRY(cudaEventRecord(k->ev_out[b], k->s_out));
+    }
+    CUDA_TRY(cudaStreamSynchronize(k->s_out));
+    CUDA_TRY(cudaStreamSynchronize(k->s_comp));
     return 0;
 }
 
 int pjg_kernel_required_memory(const pjg_kernel* k, size_t* bytes)
 {
     if (!k || !bytes) return fail(PJG_ERR_ARG, "null argument");
-    *bytes = k->problem_size * (1 + k->mech->nn + k->out_per_state) * sizeof(double) +
-             k->mech->work_bytes;
+    *bytes = (size_t)kRing * k->chunk * (1 + k->mech->nn + k->out_per_state) * sizeof(double) +
+             k->work_bytes;
     return 0;
 }
 
 int pjg_kernel_destroy(pjg_kernel* k)
 {
     if (!k) return 0;
-    cudaFree(k->d_param);
-    cudaFree(k->d_phi);
-    cudaFree(k->d_out);
-    if (k->stream) cudaStreamDestroy(k->stream);
+    if (k->s_out) cudaStreamSynchronize(k->s_out);
+    if (k->s_comp) cudaStreamSynchronize(k->s_comp);
+    free_buffers(k);
+    for (int b = 0; b < kRing; ++b) {
+        if (k->ev_in[b]) cudaEventDestroy(k->ev_in[b]);
+        if (k->ev_k[b]) cudaEventDestroy(k->ev_k[b]);
+        if (k->ev_out[b]) cudaEventDestroy(k->ev_out[b]);
+    }
+    if (k->s_in) cudaStreamDestroy(k->s_in);
+    if (k->s_comp) cudaStreamDestroy(k->s_comp);
+    if (k->s_out) cudaStreamDestroy(k->s_out);
     delete k;
     return 0;
 }

@@ -448,6 +448,19 @@ void launch(const EvalArgs& a, unsigned grid, cudaStream_t st, size_t smem_bytes
 
 }  // namespace
 
+int pjg_eval_blocks_per_sm(int kind, size_t smem_bytes)
+{
+    int b = 0;
+    cudaError_t e;
+    if (kind == 1)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, eval_kernel<1>, PJG_BLOCK, smem_bytes);
+    else if (kind == 2)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, eval_kernel<2>, PJG_BLOCK, smem_bytes);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, eval_kernel<0>, PJG_BLOCK, smem_bytes);
+    return e == cudaSuccess && b > 0 ? b : 1;
+}
+
 int pjg_launch_eval(const EvalArgs& a, int kind, void* stream, size_t smem_bytes)
 {
     if (a.n <= 0) return 0;

@@ -63,6 +63,8 @@ struct EvalArgs {
 
 // host launchers (pjg_eval.cu)
 int pjg_launch_eval(const EvalArgs& a, int kind, void* stream, size_t smem_bytes);
+// resident blocks per SM of the evaluation kernel of `kind`
+int pjg_eval_blocks_per_sm(int kind, size_t smem_bytes);
 int pjg_launch_zero(double* acc, int64_t ld, int64_t n, int nslot, void* stream);
 int pjg_fp64_probe(int blocks, int threads, int iters, double* out, void* stream);
 int pjg_launch_fexp(const double* x, double* y, int64_t n, void* stream);

@@ -161,3 +161,66 @@ def test_indices_bit_exact_device(cuda_device):
             eptr, eind = mech.pattern(order)
             assert np.array_equal(ptr, eptr) and np.array_equal(ind, eind)
 
+
+@pytest.mark.parametrize("name,n,combos", [
+    ("h2o2", 700001, [("C", "full"), ("C", "sparse"), ("F", "full"), ("F", "sparse")]),
+    ("gri30", 160000, [("F", "sparse")]),
+])
+def test_pywrap_kernel_streams_many_chunks(cuda_device, name, n, combos):
+    """The host-pointer kernel objects stream large problems through a ring of
+    three device buffers of two waves of blocks (155,648 states on 152 SMs;
+    strided copies for order F): h2o2 at 700,001 states wraps the ring.  The
+    result equals the device-pointer evaluation of the whole problem."""
+    mech = load_mech(name)
+    api = pkg("api")
+    P, phi = states(name, n, 16, True)
+    ev = evaluator(name)
+    for order, fmt in combos:
+        mod = api.pywrap(mech, order=order, conp=True, jac_format=fmt)
+        x = np.ascontiguousarray(phi if order == "C" else phi.T)
+        per = mech.nn * mech.nn if fmt == "full" else mech.jac_nnz()
+        jk = mod.PyJacobianKernel(n, 1)
+        jac = np.full(n * per, np.nan)
+        jk(P, x, jac)
+        ref = ev.jacobian(to_dev(P, cuda_device), to_dev(x, cuda_device), order=order,
+                          jac_format=fmt).cpu().numpy().ravel()
+        assert np.array_equal(jac, ref), (order, fmt)
+        rk = mod.PySpecies_RatesKernel(n, 1)
+        dphi = np.full_like(x, np.nan)
+        rk(P, x, dphi)
+        assert np.array_equal(dphi, ev.species_rates(to_dev(P, cuda_device), to_dev(x, cuda_device),
+                                                     order=order).cpu().numpy()), order
+        jk.close()
+        rk.close()
+
+
+@pytest.mark.parametrize("name,n,combos", [
+    ("h2o2", 400001, [("C", "full"), ("F", "sparse")]),
+    ("gri30", 3000, [("F", "full"), ("C", "full"), ("C", "sparse")]),
+])
+def test_pywrap_kernel_pinned_arrays(cuda_device, name, n, combos):
+    """Pinned host arrays (the copies then run asynchronously beside the
+    kernels) give the same result as the device-pointer evaluation."""
+    import torch
+    mech = load_mech(name)
+    api = pkg("api")
+    P, phi = states(name, n, 17, True)
+    ev = evaluator(name)
+    hP = torch.from_numpy(P).pin_memory().numpy()
+    for order, fmt in combos:
+        mod = api.pywrap(mech, order=order, conp=True, jac_format=fmt)
+        x = torch.from_numpy(np.ascontiguousarray(phi if order == "C" else phi.T)).pin_memory().numpy()
+        per = mech.nn * mech.nn if fmt == "full" else mech.jac_nnz()
+        jac = torch.full((n * per,), float("nan"), dtype=torch.float64, pin_memory=True).numpy()
+        jk = mod.PyJacobianKernel(n, 1)
+        jk(hP, x, jac)
+        ref = ev.jacobian(to_dev(hP, cuda_device), to_dev(x, cuda_device), order=order,
+                          jac_format=fmt).cpu().numpy().ravel()
+        assert np.array_equal(jac, ref), (order, fmt)
+        dphi = torch.full(x.shape, float("nan"), dtype=torch.float64, pin_memory=True).numpy()
+        rk = mod.PySpecies_RatesKernel(n, 1)
+        rk(hP, x, dphi)
+        assert np.array_equal(dphi, ev.species_rates(to_dev(hP, cuda_device), to_dev(x, cuda_device),
+                                                     order=order).cpu().numpy()), order
+        jk.close()
+        rk.close()
