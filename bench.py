@@ -382,6 +382,7 @@ def main():
                "h2d_bytes_per_step": int(hP.nbytes + hphi.nbytes),
                "d2h_bytes_per_step": int(hout.nbytes), "steps": k2,
                "call_ms": [round(c * 1e3, 1) for c in calls],
+               "median_call_ms": round(float(np.median(calls)) * 1e3, 1),
                "path": "%s(problem_size, work_size)(param, phi, out), pinned host arrays"
                        % type(kobj).__name__}
         kobj.close()

@@ -222,11 +222,6 @@ size_t state_bytes(const pjg_mech* m, int kind, bool c_order_jac, int nslot)
     return b;
 }
 
-bool rates_fit_smem(const pjg_mech* m)
-{
-    return (size_t)ARR_N_RATES * m->ns * PJG_BLOCK * sizeof(double) <= 200 * 1024;
-}
-
 constexpr size_t kWorkBudget = size_t(8) << 30;  // bytes of working buffer per call
 
 // States one launch can take with per_state bytes of working arrays: a whole
@@ -242,11 +237,11 @@ int64_t chunk_states(size_t per_state, int64_t n, int64_t wave)
 }
 
 // States of one full wave of the evaluation kernel of `kind` on the mechanism's device.
-int64_t wave_states(const pjg_mech* m, int kind, size_t smem_bytes)
+int64_t wave_states(const pjg_mech* m, int kind)
 {
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, m->device);
-    return (int64_t)sms * pjg_eval_blocks_per_sm(kind, smem_bytes) * PJG_BLOCK;
+    return (int64_t)sms * pjg_eval_blocks_per_sm(kind) * PJG_BLOCK;
 }
 
 int ensure_work(pjg_mech* m, size_t bytes)
@@ -273,12 +268,11 @@ void fill_common(const pjg_mech* m, EvalArgs& a)
     a.need_logP = m->need_logP;
 }
 
-// Per-state bytes of working arrays one evaluation needs (0: shared memory only).
-// The Jacobian accumulates in scratch for order 'C' (then transposed); an
-// output of order 'F' is its own accumulator.
+// Per-state bytes of working arrays one evaluation needs.  The Jacobian
+// accumulates in scratch for order 'C' (then transposed); an output of order
+// 'F' is its own accumulator.
 size_t eval_state_bytes(const pjg_mech* m, int kind, bool F, const SlotTables* t)
 {
-    if (kind == PJG_SPECIES_RATES && rates_fit_smem(m)) return 0;
     return state_bytes(m, kind, kind == PJG_JACOBIAN && !F, t ? t->nslot : 0);
 }
 
@@ -304,7 +298,6 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
         int rc = build_slots(m, F, jac_format == PJG_JAC_SPARSE, &t);
         if (rc) return rc;
     }
-    const bool smem = kind == PJG_SPECIES_RATES && rates_fit_smem(m);
     const size_t per_state = eval_state_bytes(m, kind, F, t);
     int64_t ch;
     double* work = ext_work;
@@ -313,7 +306,7 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
         if (ch < PJG_BLOCK && ch < n) return fail(PJG_ERR_ARG, "working buffer too small");
         ch = std::min<int64_t>(std::max<int64_t>(ch, 1), n);
     } else {
-        ch = chunk_states(per_state, n, wave_states(m, kind, 0));
+        ch = chunk_states(per_state, n, wave_states(m, kind));
         if (per_state) {
             int rc = ensure_work(m, per_state * (size_t)ch);
             if (rc) return rc;
@@ -336,10 +329,8 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
             a.phi_ss = NN;
             a.phi_sj = 1;
         }
-        a.use_smem = smem;
         a.scratch = work;
         a.sc_ld = ch;
-        size_t smem_bytes = smem ? (size_t)ARR_N_RATES * m->ns * PJG_BLOCK * sizeof(double) : 0;
         if (kind == PJG_SPECIES_RATES) {
             a.dphi = F ? out + off : out + off * NN;
             a.dphi_ss = a.phi_ss;
@@ -382,7 +373,7 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
             cudaEventCreate(&e1);
             cudaEventRecord(e0, st);
         }
-        rc = pjg_launch_eval(a, kind, st, smem_bytes);
+        rc = pjg_launch_eval(a, kind, st);
         if (rc) return fail(PJG_ERR_CUDA, "kernel launch failed: %s",
                             cudaGetErrorString(cudaGetLastError()));
         g_launches.fetch_add(1);
@@ -713,7 +704,7 @@ int pjg_kernel_resize(pjg_kernel* k, size_t problem_size, size_t work_size)
 {
     if (!k) return fail(PJG_ERR_ARG, "null kernel");
     k->work_size = work_size;
-    const int64_t wave = wave_states(k->mech, PJG_JACOBIAN, 0);
+    const int64_t wave = wave_states(k->mech, PJG_JACOBIAN);
     const int64_t chunk = std::min<int64_t>((int64_t)problem_size, PJG_CHUNK_WAVES * wave);
     if (chunk == k->chunk && k->d_phi[0]) {
         k->problem_size = problem_size;

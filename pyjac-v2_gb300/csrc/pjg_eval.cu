@@ -51,12 +51,16 @@ struct SV {
     __device__ __forceinline__ double& operator[](int k) const { return b[(int64_t)k * st]; }
 };
 
+#ifndef PJG_VJP_MINB
+#define PJG_VJP_MINB 3  // resident 128-thread blocks per SM requested for the J^T v kernel
+#endif
+
 #ifndef PJG_JAC_MINB
 #define PJG_JAC_MINB 4  // resident 128-thread blocks per SM requested for the Jacobian kernel
 #endif
 
 template <int KIND>  // 0 species rates, 1 Jacobian, 2 J^T v
-__global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND == 2 ? 3 : 4))
+__global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND == 2 ? PJG_VJP_MINB : 4))
     eval_kernel(const EvalArgs a)
 {
     __shared__ double etab[PJG_EXP_TAB];
@@ -67,11 +71,8 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     constexpr bool JAC = KIND == 1;
     constexpr bool VJP = KIND == 2;
     constexpr bool DER = KIND >= 1;  // derivative terms needed
-    extern __shared__ double smem[];
     const int ns = a.ns, last = ns - 1;
     auto arr = [&](int which) -> SV {
-        if (a.use_smem)
-            return SV{smem + (int64_t)which * ns * blockDim.x + threadIdx.x, (int64_t)blockDim.x};
         return SV{a.scratch + (int64_t)which * ns * a.sc_ld + s, a.sc_ld};
     };
     SV conc = arr(ARR_CONC), bk = arr(ARR_B), wdot = arr(ARR_WDOT);
@@ -85,15 +86,13 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         dcpa = arr(ARR_DCP);
         ha = arr(ARR_H);
     }
-    // Per-state arrays in global scratch accumulate with fire-and-forget
-    // reductions (as the Jacobian does) and are read back from L2 after a
-    // fence; in shared memory they are plain read-modify-writes.
-    const bool gl = !a.use_smem;
-    auto accum = [&](const SV& v, int k, double x) {
-        if (gl) atomicAdd(&v[k], x);
-        else v[k] += x;
-    };
-    auto rd = [&](const SV& v, int k) -> double { return gl ? __ldcg(&v[k]) : v[k]; };
+    // The per-state arrays live in global scratch (state-innermost, so a
+    // warp's accesses are coalesced) and stay in L1/L2: shared memory would
+    // hold too few states per SM to keep the FP64 pipe busy.  Accumulators
+    // take fire-and-forget reductions, performed in L2, and are read back
+    // from L2 after a fence.
+    auto accum = [&](const SV& v, int k, double x) { atomicAdd(&v[k], x); };
+    auto rd = [&](const SV& v, int k) -> double { return __ldcg(&v[k]); };
     const bool conp = a.conp;
     const double* ph = a.phi + s * a.phi_ss;
     const double T = ph[0];
@@ -180,24 +179,11 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         const int flags = h.flags, nsp = h.nsp, thd_off = h.thd_off, thd_cnt = h.thd_cnt;
         const unsigned* ent = h.ent;
         const double* p = h.p;
-        if (gl) {
 #pragma unroll
-            for (int e = 0; e < PJG_MAXSP; ++e) {
-                if (e >= nsp) break;
-                const int nu = ent_nur(ent[e]) - ent_nuf(ent[e]);
-                if (nu != 0) accum(wdot, ent_spec(ent[e]), nux(nu, o.net));
-            }
-        } else {
-            // participants are distinct species: load all, then update
-            double wv[PJG_MAXSP];
-#pragma unroll
-            for (int e = 0; e < PJG_MAXSP; ++e)
-                if (e < nsp) wv[e] = wdot[ent_spec(ent[e])];
-#pragma unroll
-            for (int e = 0; e < PJG_MAXSP; ++e) {
-                if (e >= nsp) break;
-                wdot[ent_spec(ent[e])] = addnu(wv[e], ent_nur(ent[e]) - ent_nuf(ent[e]), o.net);
-            }
+        for (int e = 0; e < PJG_MAXSP; ++e) {
+            if (e >= nsp) break;
+            const int nu = ent_nur(ent[e]) - ent_nuf(ent[e]);
+            if (nu != 0) accum(wdot, ent_spec(ent[e]), nux(nu, o.net));
         }
         if (!DER) continue;
 
@@ -281,7 +267,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         }
     }
 
-    if (gl) __threadfence();
+    __threadfence();
 
     // ------------------------------------------- temperature and E rates
     double upper = 0.0, lower = 0.0;
@@ -438,36 +424,33 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
 namespace {
 
 template <int KIND>
-void launch(const EvalArgs& a, unsigned grid, cudaStream_t st, size_t smem_bytes)
+void launch(const EvalArgs& a, unsigned grid, cudaStream_t st)
 {
-    if (smem_bytes > 48 * 1024)
-        cudaFuncSetAttribute(eval_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem_bytes);
-    eval_kernel<KIND><<<grid, PJG_BLOCK, smem_bytes, st>>>(a);
+    eval_kernel<KIND><<<grid, PJG_BLOCK, 0, st>>>(a);
 }
 
 }  // namespace
 
-int pjg_eval_blocks_per_sm(int kind, size_t smem_bytes)
+int pjg_eval_blocks_per_sm(int kind)
 {
     int b = 0;
     cudaError_t e;
     if (kind == 1)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, eval_kernel<1>, PJG_BLOCK, smem_bytes);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, eval_kernel<1>, PJG_BLOCK, 0);
     else if (kind == 2)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, eval_kernel<2>, PJG_BLOCK, smem_bytes);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, eval_kernel<2>, PJG_BLOCK, 0);
     else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, eval_kernel<0>, PJG_BLOCK, smem_bytes);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, eval_kernel<0>, PJG_BLOCK, 0);
     return e == cudaSuccess && b > 0 ? b : 1;
 }
 
-int pjg_launch_eval(const EvalArgs& a, int kind, void* stream, size_t smem_bytes)
+int pjg_launch_eval(const EvalArgs& a, int kind, void* stream)
 {
     if (a.n <= 0) return 0;
     cudaStream_t st = (cudaStream_t)stream;
     const unsigned grid = (unsigned)((a.n + PJG_BLOCK - 1) / PJG_BLOCK);
-    if (kind == 1) launch<1>(a, grid, st, smem_bytes);
-    else if (kind == 2) launch<2>(a, grid, st, smem_bytes);
-    else launch<0>(a, grid, st, smem_bytes);
+    if (kind == 1) launch<1>(a, grid, st);
+    else if (kind == 2) launch<2>(a, grid, st);
+    else launch<0>(a, grid, st);
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }

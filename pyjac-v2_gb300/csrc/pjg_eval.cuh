@@ -38,11 +38,10 @@ struct EvalArgs {
     int64_t phi_ss, phi_sj;  // element (s, j) at phi[s * phi_ss + j * phi_sj]
     double* dphi;            // optional
     int64_t dphi_ss, dphi_sj;
-    // per-state arrays: global scratch (arr a, species k, state s at
-    // scratch[(a * ns + k) * sc_ld + s]) unless use_smem
+    // per-state arrays in global scratch: array a, species k, state s at
+    // scratch[(a * ns + k) * sc_ld + s]
     double* scratch;
     int64_t sc_ld;
-    int use_smem;
     // Jacobian accumulator: acc[slot * acc_ld + s]
     double* acc;
     int64_t acc_ld;
@@ -62,9 +61,9 @@ struct EvalArgs {
 };
 
 // host launchers (pjg_eval.cu)
-int pjg_launch_eval(const EvalArgs& a, int kind, void* stream, size_t smem_bytes);
+int pjg_launch_eval(const EvalArgs& a, int kind, void* stream);
 // resident blocks per SM of the evaluation kernel of `kind`
-int pjg_eval_blocks_per_sm(int kind, size_t smem_bytes);
+int pjg_eval_blocks_per_sm(int kind);
 int pjg_launch_zero(double* acc, int64_t ld, int64_t n, int nslot, void* stream);
 int pjg_fp64_probe(int blocks, int threads, int iters, double* out, void* stream);
 int pjg_launch_fexp(const double* x, double* y, int64_t n, void* stream);

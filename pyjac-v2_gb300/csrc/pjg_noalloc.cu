@@ -120,10 +120,9 @@ extern "C" int pjg_vjp_noalloc(pjg_mech* mech, int64_t n, char order, int conp, 
             a.v = v + off * NN;
             a.vjp = out + off * NN;
         }
-        a.use_smem = 0;
         a.scratch = scratch;
         a.sc_ld = chunk;
-        rc = pjg_launch_eval(a, 2, stream, 0);
+        rc = pjg_launch_eval(a, 2, stream);
         if (rc) return pjg_internal_fail(PJG_ERR_CUDA, "pjg_vjp_noalloc: kernel launch failed");
         pjg_internal_count_launch();
     }
