@@ -4,13 +4,17 @@ Workload (the headline configuration): GRI-Mech 3.0 (53 species, 325
 reactions), 1,048,576 seeded synthetic states (T ~ U(800, 2200) K,
 P log-uniform 1-25 atm, X ~ Dirichlet(0.5) floored at 1e-12, V = 1 m^3),
 constant pressure, F data order, dense 54 x 54 Jacobian.  One step = one
-Jacobian evaluation of all states (pjg_jacobian).  Inputs (432 MB) and outputs
-(24.9 GB) are larger than L2, so no flush is needed between steps.
+Jacobian evaluation of all states (pjg_jacobian).  Inputs (453 MB) and outputs
+(24.5 GB) are larger than L2, so no flush is needed between steps.
+
+Other configurations: ``--mech h2o2`` (H2/O2), ``--mech synthetic500`` (the
+seeded 500-species, 2,500-reaction mechanism), ``--format sparse``,
+``--order C``, ``--kernel rates|vjp``, ``--states N``.
 
 Prints one JSON line (rank 0).  ``--impl reference`` times the reference's CPU
 implementation of the same path on the host cores instead: the shim-compiled
-shipped GRI kernels in oracle/_ref when they load here, else the C oracle
-(the CPU restatement of the reference) with OpenMP on all cores.
+shipped GRI or H2/O2 kernels in oracle/_ref when they load here, else the C
+oracle (the CPU restatement of the reference) with OpenMP on all cores.
 """
 import argparse
 import ctypes
@@ -53,6 +57,28 @@ def pkg(sub=None):
 def load_gri():
     return pkg().load_mechanism(os.path.join(ROOT, "data", "grimech30.inp"),
                                 os.path.join(ROOT, "data", "thermo30.dat"))
+
+
+# --mech: the benchmark configurations' mechanisms, their label and the
+# reference's shipped kernels for the CPU baseline (None: the C oracle port)
+MECHS = {
+    "gri30": ("GRI-30", "ch4", "grimech30 (53 species, 325 reactions)"),
+    "h2o2": ("H2/O2", "h2o2", "h2o2 (9 species, 28 reactions)"),
+    "synthetic500": ("synthetic-500", None, "seeded synthetic (500 species, 2,500 reactions)"),
+}
+
+
+def load_mech(name):
+    if name == "gri30":
+        return load_gri()
+    if name == "h2o2":
+        return pkg().load_mechanism(os.path.join(ROOT, "data", "h2o2.inp"))
+    import tempfile
+    path = os.path.join(tempfile.gettempdir(), "pyjac_gb300_synthetic500_seed0.inp")
+    if not os.path.exists(path):
+        pkg("mech.synthetic").write(path + ".tmp")  # defaults: 500 species, 2,500 reactions
+        os.replace(path + ".tmp", path)
+    return pkg().load_mechanism(path)
 
 
 class ClockSampler(object):
@@ -115,7 +141,7 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def cpu_reference_run(mech, n_sample, steps, seed=1, warmup=1):
+def cpu_reference_run(mech, n_sample, steps, seed=1, warmup=1, mech_name="gri30"):
     """Time the reference's CPU implementation: states/s and a description."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     orc = importlib.import_module("oracle")
@@ -123,12 +149,14 @@ def cpu_reference_run(mech, n_sample, steps, seed=1, warmup=1):
     P, phi = states.draw_states(mech.n_species, n_sample, seed=seed, x_floor=1e-12)
     threads = cpu_threads()
     kind, fn = None, None
-    if orc.RefKernels.available("ch4"):
+    label, shipped, _ = MECHS[mech_name]
+    if shipped and orc.RefKernels.available(shipped):
         try:
-            ref = orc.RefKernels("ch4")
+            ref = orc.RefKernels(shipped)
             phiF = np.ascontiguousarray(phi.T)
             kind = "reference"
-            desc = "reference shipped GRI-30 kernels (examples/opencl/ch4, sparse CCS), shim-compiled"
+            desc = ("reference shipped %s kernels (examples/opencl/%s, %s), shim-compiled"
+                    % (label, shipped, "sparse CCS" if shipped == "ch4" else "dense"))
 
             def fn():
                 ref.jacobian_F(P, phiF, nthreads=threads)
@@ -150,7 +178,7 @@ def cpu_reference_run(mech, n_sample, steps, seed=1, warmup=1):
         ts.append(time.perf_counter() - t0)
     sec = float(np.mean(ts))
     return {"value": n_sample / sec, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": "%d GRI-30 states per step, %s" % (n_sample, desc)}, sec
+            "sample": "%d %s states per step, %s" % (n_sample, label, desc)}, sec
 
 
 def surrogate_bench(mech, ev, dev, n_train, epochs, n_eval, log=None):
@@ -217,15 +245,17 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    mech = load_gri()
+    mech = load_mech(args.mech)
     n = args.cpu_sample
-    cb, sec = cpu_reference_run(mech, n, args.steps, warmup=args.warmup)
-    out = {"metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
+    cb, sec = cpu_reference_run(mech, n, args.steps, warmup=args.warmup, mech_name=args.mech)
+    out = {"metric": METRIC.replace("GRI-30", MECHS[args.mech][0]), "value": cb["value"],
+           "unit": UNIT, "impl": "reference",
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "GRI-Mech 3.0 FP64 Jacobian, %d states per step on host cores" % n,
-                      "mechanism": "grimech30", "states": n, "conp": True},
+           "config": {"workload": "%s FP64 Jacobian, %d states per step on host cores"
+                                  % (MECHS[args.mech][0], n),
+                      "mechanism": MECHS[args.mech][2], "states": n, "conp": True},
            "cpu_baseline": cb,
            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
@@ -242,16 +272,22 @@ def main():
     ap.add_argument("--states", type=int, default=1 << 20)
     ap.add_argument("--format", default="full", choices=["full", "sparse"])
     ap.add_argument("--order", default="F", choices=["C", "F"])
-    ap.add_argument("--cpu-sample", type=int, default=65536)
+    ap.add_argument("--cpu-sample", type=int, default=None,
+                    help="states per CPU-baseline step (default: about 10 s of work on 16 cores "
+                         "for the reference's code; 2,048 for the 500-species oracle port)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--sur-train", type=int, default=1 << 22)
     ap.add_argument("--sur-epochs", type=int, default=12)
     ap.add_argument("--sur-eval", type=int, default=1 << 22)
+    ap.add_argument("--mech", default="gri30", choices=sorted(MECHS),
+                    help="mechanism: GRI-Mech 3.0 (headline), H2/O2, or the 500-species synthetic")
     ap.add_argument("--kernel", default="jacobian", choices=sorted(KERNELS),
                     help="evaluation timed: the Jacobian (headline), species rates or J^T v")
     args = ap.parse_args()
+    if args.cpu_sample is None:
+        args.cpu_sample = {"gri30": 524288, "h2o2": 2097152, "synthetic500": 2048}[args.mech]
     if args.impl == "reference":
         return run_reference(args)
 
@@ -267,11 +303,13 @@ def main():
     lib = pkg("_lib")
     api = pkg("api")
     states = pkg("states")
-    mech = load_gri()
+    mech = load_mech(args.mech)
     ev = api.Evaluator(mech)
     n = args.states
     nn = mech.nn
     metric, unit, kname = KERNELS[args.kernel]
+    label = MECHS[args.mech][0]
+    metric = metric.replace("GRI-30", label)
     if args.kernel == "jacobian":
         n_out = nn * nn if args.format == "full" else mech.jac_nnz()
         n_in = nn + 1
@@ -337,6 +375,8 @@ def main():
             hbm_peak = float(json.load(fh).get("hbm_gbs", hbm_peak))
         peak_src = "measured"
     key = "%s_%s_%s" % (args.kernel, args.format if args.kernel == "jacobian" else "na", args.order)
+    if args.mech != "gri30":
+        key = args.mech + "_" + key
     counts = {}
     if os.path.exists(COUNTS):
         with open(COUNTS) as fh:
@@ -390,10 +430,10 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu and args.kernel == "jacobian":
-        cpu, _ = cpu_reference_run(mech, args.cpu_sample, 1)
+        cpu, _ = cpu_reference_run(mech, args.cpu_sample, 1, mech_name=args.mech)
 
     sur = None
-    if not args.no_surrogate and args.kernel == "jacobian":
+    if not args.no_surrogate and args.kernel == "jacobian" and args.mech == "gri30":
         del out
         torch.cuda.empty_cache()
         sur = surrogate_bench(mech, ev, dev, args.sur_train, args.sur_epochs, args.sur_eval,
@@ -404,12 +444,14 @@ def main():
                 "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic",
-                "config": {"workload": ("GRI-Mech 3.0 %s FP64 Jacobian, %s order, %d states"
-                                        % ("dense" if args.format == "full" else "sparse CCS/CRS",
+                "config": {"workload": ("%s %s FP64 Jacobian, %s order, %d states"
+                                        % (label, "dense" if args.format == "full" else
+                                           ("sparse CCS" if args.order == "F" else "sparse CRS"),
                                            args.order, n)) if args.kernel == "jacobian" else
-                           ("GRI-Mech 3.0 FP64 %s, %s order, %d states"
-                            % ("species rates" if args.kernel == "rates" else "J^T v", args.order, n)),
-                           "mechanism": "grimech30 (53 species, 325 reactions)",
+                           ("%s FP64 %s, %s order, %d states"
+                            % (label, "species rates" if args.kernel == "rates" else "J^T v",
+                               args.order, n)),
+                           "mechanism": MECHS[args.mech][2],
                            "states": n, "order": args.order, "jac_format": args.format,
                            "conp": True,
                            "l2": "inputs %.0f MB and outputs %.0f MB, both larger than L2 (126 MB): "

@@ -100,6 +100,7 @@ constexpr int kRing = 3;
 #ifndef PJG_CHUNK_WAVES
 #define PJG_CHUNK_WAVES 2
 #endif
+constexpr size_t kKernelBudget = size_t(32) << 30;  // device bytes of one kernel object
 
 struct pjg_kernel {
     pjg_mech* mech = nullptr;
@@ -225,14 +226,23 @@ size_t state_bytes(const pjg_mech* m, int kind, bool c_order_jac, int nslot)
 constexpr size_t kWorkBudget = size_t(8) << 30;  // bytes of working buffer per call
 
 // States one launch can take with per_state bytes of working arrays: a whole
-// number of waves of resident blocks where the budget allows (a launch of a
-// fraction of a wave takes as long as a full wave), at most n.
+// number of waves of resident blocks within the budget (a launch of a
+// fraction of a wave takes as long as a full wave).  Where one wave needs
+// more than the budget (large mechanisms in order 'C'), a full wave if half
+// the free device memory holds it, else as much as fits.  At most n.
 int64_t chunk_states(size_t per_state, int64_t n, int64_t wave)
 {
     if (per_state == 0) return n;
     int64_t c = (int64_t)(kWorkBudget / per_state);
-    if (c >= wave) c = c / wave * wave;
-    else c = std::max<int64_t>(PJG_BLOCK, c / PJG_BLOCK * PJG_BLOCK);
+    if (c >= wave) {
+        c = c / wave * wave;
+    } else {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
+        const int64_t fit = (int64_t)(free_b / 2 / per_state);
+        c = std::max<int64_t>(c, std::min<int64_t>(fit, wave));
+        c = std::max<int64_t>(PJG_BLOCK, c / PJG_BLOCK * PJG_BLOCK);
+    }
     return std::min<int64_t>(c, n);
 }
 
@@ -704,8 +714,21 @@ int pjg_kernel_resize(pjg_kernel* k, size_t problem_size, size_t work_size)
 {
     if (!k) return fail(PJG_ERR_ARG, "null kernel");
     k->work_size = work_size;
-    const int64_t wave = wave_states(k->mech, PJG_JACOBIAN);
-    const int64_t chunk = std::min<int64_t>((int64_t)problem_size, PJG_CHUNK_WAVES * wave);
+    pjg_mech* m = k->mech;
+    SlotTables* t = nullptr;
+    if (k->kind == PJG_JACOBIAN && problem_size) {
+        int rc = build_slots(m, k->order == 'F', k->jac_format == PJG_JAC_SPARSE, &t);
+        if (rc) return rc;
+    }
+    const size_t nn = m->nn;
+    const size_t per_state = eval_state_bytes(m, k->kind, k->order == 'F', t);
+    // two waves per chunk, fewer where the ring and working arrays would pass
+    // the kernel object's budget (large mechanisms)
+    const size_t ring_state = kRing * (1 + nn + k->out_per_state) * sizeof(double) + per_state;
+    int64_t chunk = std::min<int64_t>((int64_t)problem_size,
+                                      PJG_CHUNK_WAVES * wave_states(m, PJG_JACOBIAN));
+    if ((size_t)chunk * ring_state > kKernelBudget)
+        chunk = std::max<int64_t>(PJG_BLOCK, (int64_t)(kKernelBudget / ring_state) / PJG_BLOCK * PJG_BLOCK);
     if (chunk == k->chunk && k->d_phi[0]) {
         k->problem_size = problem_size;
         return 0;
@@ -713,19 +736,11 @@ int pjg_kernel_resize(pjg_kernel* k, size_t problem_size, size_t work_size)
     free_buffers(k);
     k->problem_size = problem_size;
     if (problem_size == 0) return 0;
-    pjg_mech* m = k->mech;
-    SlotTables* t = nullptr;
-    if (k->kind == PJG_JACOBIAN) {
-        int rc = build_slots(m, k->order == 'F', k->jac_format == PJG_JAC_SPARSE, &t);
-        if (rc) return rc;
-    }
-    const size_t nn = m->nn;
     for (int b = 0; b < kRing; ++b) {
         CUDA_TRY(cudaMalloc((void**)&k->d_param[b], chunk * sizeof(double)));
         CUDA_TRY(cudaMalloc((void**)&k->d_phi[b], chunk * nn * sizeof(double)));
         CUDA_TRY(cudaMalloc((void**)&k->d_out[b], chunk * k->out_per_state * sizeof(double)));
     }
-    const size_t per_state = eval_state_bytes(m, k->kind, k->order == 'F', t);
     const int64_t padded = (chunk + PJG_BLOCK - 1) / PJG_BLOCK * PJG_BLOCK;
     k->work_bytes = per_state * (size_t)padded;
     if (k->work_bytes) CUDA_TRY(cudaMalloc((void**)&k->work, k->work_bytes));

@@ -41,7 +41,17 @@ _cache = {}
 
 def load_mech(name):
     if name not in _cache:
-        if name == "synthetic_small":
+        if name == "synthetic500":
+            # the 500-species, 2,500-reaction benchmark mechanism (seed 0),
+            # generated once per machine outside the repository
+            import tempfile
+            syn = pkg("mech.synthetic")
+            path = os.path.join(tempfile.gettempdir(), "pyjac_gb300_synthetic500_seed0.inp")
+            if not os.path.exists(path):
+                syn.write(path + ".tmp")
+                os.replace(path + ".tmp", path)
+            _cache[name] = pkg().load_mechanism(path)
+        elif name == "synthetic_small":
             syn = pkg("mech.synthetic")
             path = os.path.join(GOLDEN, "synthetic_small.inp")
             if not os.path.exists(path):
