@@ -57,7 +57,12 @@ enum pjg_jac_format { PJG_JAC_FULL = 0, PJG_JAC_SPARSE = 1 };
 typedef struct pjg_tables {
     int32_t ns;              /* species, bath gas last */
     int32_t nr;              /* reactions */
-    int32_t flags;           /* bit 0: mechanism has PLOG/Chebyshev (needs ln P) */
+    int32_t flags;           /* bit 0: mechanism has PLOG/Chebyshev (needs ln P);
+                              * bit 1: the 'approximate' Jacobian type, which omits
+                              * the bath-gas terms d n_Ns / d n_j of the species
+                              * columns (create_jacobian.py:186-190, :3578-3582,
+                              * :4187-4191); the pattern arrays must be the
+                              * approximate type's */
     const void* rxn;         /* nr reaction records, 192 bytes each */
     const double* species;   /* ns species records, 16 doubles each */
     const int32_t* thd_spec; /* third-body species lists */
@@ -97,6 +102,14 @@ int pjg_species_rates(pjg_mech* mech, int64_t n, char order, int conp, const dou
                       const double* phi, double* dphi, void* stream);
 int pjg_jacobian(pjg_mech* mech, int64_t n, char order, int conp, int jac_format,
                  const double* param, const double* phi, double* jac, void* stream);
+/* Species thermo, the chem_utils kernel type (pyjac/core/rate_subs.py
+ * write_chem_utils :3391-3444; examples/opencl/ch4/chem_utils.ocl:49): at
+ * the guarded temperature T = min(max(phi_T, 100 K), 10,000 K) of each state,
+ * cp, h and the Gibbs function b of every species (cv, u and b when conp is
+ * 0).  Each output holds Ns values per state: [i*Ns + k] for order 'C',
+ * [i + n*k] for 'F'.  phi as above (only T is read). */
+int pjg_chem_utils(pjg_mech* mech, int64_t n, char order, int conp, const double* phi, double* cp,
+                   double* h, double* b, void* stream);
 /* Vector-Jacobian product out = J^T v (dense J of kernel order; v, out have NN
  * entries per state in `order`).  No reference counterpart: the adjoint used
  * by the torch wdot autograd.Function. */
@@ -155,6 +168,18 @@ int pjg_mlp_linear(const void* X, int64_t ldx, const void* W, int64_t ldw, int64
 int pjg_mlp_wgrad(const void* A, int64_t lda, const void* B, int64_t ldb, int Mo, int No,
                   int64_t Kb, float* C, int64_t ldc, void* stream);
 int pjg_mlp_status(int clear);
+
+/* Binary initial-condition files: the reference's read_initial_conditions
+ * (pyjac/kernel_utils/common/read_initial_conditions.cpp.in:30-116).  One
+ * record of NN + 1 doubles per state, C order on disk:
+ * [T, param, phi_1 (extra variable), n_0 .. n_{Ns-2}], param = P (conp) or V
+ * (conv).  Read fills param[n] and phi in `order`; a file that is missing or
+ * holds fewer than n records returns PJG_ERR_ARG with a message (the reference
+ * exits the process).  Write is the inverse.  Host memory, host code. */
+int pjg_read_initial_conditions(const char* filename, int64_t n, int32_t nn, char order,
+                                double* param, double* phi);
+int pjg_write_initial_conditions(const char* filename, int64_t n, int32_t nn, char order,
+                                 const double* param, const double* phi);
 
 /* Copy the last error message of this thread into buf (always NUL-terminated). */
 int pjg_last_error(char* buf, size_t len);

@@ -59,7 +59,8 @@ class _OrcMech(ctypes.Structure):
                 ("fall_troe", _I), ("fall_sri", _I),
                 ("troe_a", _D), ("troe_T1", _D), ("troe_T2", _D), ("troe_T3", _D),
                 ("sri_a", _D), ("sri_b", _D), ("sri_c", _D), ("sri_d", _D), ("sri_e", _D),
-                ("a_lo", _D), ("a_hi", _D), ("T_mid", _D), ("mw_post", _D)]
+                ("a_lo", _D), ("a_hi", _D), ("T_mid", _D), ("mw_post", _D),
+                ("jac_approx", ctypes.c_int)]
 
 
 def _offsets(counts):
@@ -76,6 +77,9 @@ class Oracle(object):
             fn.restype = ctypes.c_int
             fn.argtypes = [ctypes.POINTER(_OrcMech), ctypes.c_long, ctypes.c_int, _D, _D, _D,
                            ctypes.c_int]
+        self._lib.orc_chem_utils.restype = ctypes.c_int
+        self._lib.orc_chem_utils.argtypes = [ctypes.POINTER(_OrcMech), ctypes.c_long, ctypes.c_int,
+                                             _D, _D, _D, _D]
         self.mech = mech
         v = mech.val
         Ns, Nr = v["Ns"], v["Nr"]
@@ -158,6 +162,7 @@ class Oracle(object):
         m.a_hi = D(v["thermo"]["a_hi"])
         m.T_mid = D(v["thermo"]["T_mid"])
         m.mw_post = D(v["mw_post"])
+        m.jac_approx = int(getattr(mech, "jac_type", "exact") == "approximate")
         self._m = m
         self.nn = Ns + 1
 
@@ -185,6 +190,17 @@ class Oracle(object):
         n = np.asarray(phi).shape[0]
         out = np.empty((n, self.nn, self.nn))
         return self._call(self._lib.orc_jacobian, param, phi, out, conp, nthreads)
+
+    def chem_utils(self, phi, conp=True):
+        """phi (n, NN) C order -> (cp or cv, h or u, b), each (n, Ns)."""
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        n, ns = phi.shape[0], self.nn - 1
+        out = [np.empty((n, ns)) for _ in range(3)]
+        rc = self._lib.orc_chem_utils(ctypes.byref(self._m), n, int(bool(conp)), phi.ctypes.data_as(_D),
+                                      *[o.ctypes.data_as(_D) for o in out])
+        if rc != 0:
+            raise RuntimeError("oracle returned %d" % rc)
+        return tuple(out)
 
 
 class RefKernels(object):
@@ -225,3 +241,14 @@ class RefKernels(object):
                                np.ascontiguousarray(phi_F).ctypes.data_as(_D),
                                out.ctypes.data_as(_D), int(nthreads))
         return out
+
+    def chem_utils_F(self, phi_F, nthreads=0):
+        """The shipped chem_utils kernel: (cp, h, b), each (Ns, n) F order."""
+        n = phi_F.shape[1]
+        out = [np.zeros((self.ns, n)) for _ in range(3)]
+        fn = self._lib.ref_chem_utils
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.c_long, _D, _D, _D, _D, ctypes.c_int]
+        fn(n, np.ascontiguousarray(phi_F).ctypes.data_as(_D), *[o.ctypes.data_as(_D) for o in out],
+           int(nthreads))
+        return tuple(out)

@@ -440,7 +440,7 @@ static void eval_jacobian(const orc_mech* m, int conp, double param, const doubl
                 JAC(sk + 2, sj + 2) += (kf * Sf + -1.0 * kr * Sr) * ci * nuk;
             }
         }
-        if (has_ns) {
+        if (has_ns && !m->jac_approx) {
             for (int ek = o0; ek < o1; ++ek) {
                 const int sk = m->net_spec[ek];
                 if (sk == last) continue;
@@ -500,7 +500,7 @@ static void eval_jacobian(const orc_mech* m, int conp, double param, const doubl
                 JAC(sk + 2, sj + 2) += nuk * dci * R * fac;
             }
         }
-        if (ns_listed) {
+        if (ns_listed && !m->jac_approx) {
             double dci = ttype == 2 ? -1.0 : (ttype == 1 ? 1.0 + -1.0 * ns_eff : 0.0);
             for (int ek = o0; ek < o1; ++ek) {
                 const int sk = m->net_spec[ek];
@@ -866,4 +866,28 @@ int orc_rates_scale(const orc_mech* m, long n, int conp, const double* param, co
                     double* scale, int nthreads)
 {
     return run(m, n, conp, param, phi, scale, nthreads, 2);
+}
+
+int orc_chem_utils(const orc_mech* m, long n, int conp, const double* phi, double* cp,
+                   double* h, double* b)
+{
+    if (!m || n < 0 || (n && (!phi || !cp || !h || !b))) return -1;
+    const int ns = m->ns, NN = ns + 1;
+    for (long i = 0; i < n; ++i) {
+        /* the temperature guard of polyfit_kernel_gen (TemperatureGuard) */
+        const double Tc = fmin(10000.0, fmax(100.0, phi[i * NN]));
+        const double logT = log(Tc), Tinv = 1.0 / Tc;
+        for (int k = 0; k < ns; ++k) {
+            const double* a;
+            thermo_coeffs(m, k, Tc, &a);
+            const double cpoly = Tc * (Tc * (Tc * (Tc * a[4] + a[3]) + a[2]) + a[1]) + a[0];
+            const double hpoly =
+                Tc * (Tc * (Tc * (Tc * (Tc * a[4] / 5.0 + a[3] / 4.0) + a[2] / 3.0) + a[1] / 2.0) + a[0]);
+            cp[i * ns + k] = conp ? RU * cpoly : RU * (cpoly - 1.0);
+            h[i * ns + k] = conp ? RU * (hpoly + a[5]) : RU * (hpoly - Tc + a[5]);
+            b[i * ns + k] = Tc * (Tc * (Tc * (Tc * a[4] / 20.0 + a[3] / 12.0) + a[2] / 6.0) + a[1] / 2.0) +
+                            (a[0] + -1.0) * logT + -1.0 * a[0] + a[6] + -1.0 * a[5] * Tinv;
+        }
+    }
+    return 0;
 }

@@ -61,6 +61,10 @@ typedef struct orc_mech {
     const double *a_lo, *a_hi;  /* [ns][7] */
     const double* T_mid;
     const double* mw_post;      /* ns - 1 */
+    /* 1: the 'approximate' Jacobian type, without the bath-gas ("_ns")
+     * terms in the species columns (create_jacobian.py:186-190, :3578-3582,
+     * :4187-4191) */
+    int jac_approx;
 } orc_mech;
 
 /* phi: [n][ns+1] = (T, V or P, n_0 .. n_{ns-2}); param: P (conp) or V (conv).
@@ -76,6 +80,12 @@ int orc_jacobian(const orc_mech* m, long n, int conp, const double* param,
  * quantity. */
 int orc_rates_scale(const orc_mech* m, long n, int conp, const double* param,
                     const double* phi, double* scale, int nthreads);
+/* Species thermo of the chem_utils kernel type (rate_subs.py write_chem_utils
+ * :3391-3444, polyfit_kernel_gen :3281-3388): at the guarded T = phi[i][0],
+ * cp (cv for conv), h (u) and the Gibbs function b of every species,
+ * out[i][k] for k < ns. */
+int orc_chem_utils(const orc_mech* m, long n, int conp, const double* phi, double* cp,
+                   double* h, double* b);
 
 #ifdef __cplusplus
 }

@@ -93,4 +93,42 @@ int ref_jacobian(long n, const double* P, const double* phi, double* jac, int nt
     return run(1, n, P, phi, jac, nthreads);
 }
 
+/* the shipped chem_utils kernel (eval_cp, eval_h, eval_b): cp, h and the
+ * Gibbs function b of every species at T = phi[i] (guarded), F order
+ * out[i + n * k] for k < NS */
+int ref_chem_utils(long n, const double* phi, double* cp, double* h, double* b, int nthreads)
+{
+    if (n <= 0) return 0;
+    const long nchunks = (n + 127) / 128;
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel num_threads(nthreads)
+    {
+        std::vector<double> rwk((size_t)REF_RWK, 0.0);
+        std::vector<double> phi_l(128 * (size_t)NN), cp_l(128 * (size_t)NS), h_l(128 * (size_t)NS),
+            b_l(128 * (size_t)NS);
+        clshim::gid = 0;
+        clshim::ngroups = 1;
+#pragma omp for schedule(dynamic, 4)
+        for (long c = 0; c < nchunks; ++c) {
+            const long off = c * 128;
+            const int cnt = (int)((n - off) < 128 ? (n - off) : 128);
+            for (int l = 0; l < 128; ++l) {
+                const long s = off + (l < cnt ? l : 0);
+                for (int j = 0; j < NN; ++j) phi_l[l + 128 * j] = phi[s + n * j];
+            }
+            for (int l = 0; l < 128; ++l) {
+                clshim::lid = l;
+                chem_utils(nullptr, b_l.data(), phi_l.data(), h_l.data(), cp_l.data(), rwk.data());
+            }
+            for (int l = 0; l < cnt; ++l)
+                for (int k = 0; k < NS; ++k) {
+                    cp[off + l + n * k] = cp_l[l + 128 * k];
+                    h[off + l + n * k] = h_l[l + 128 * k];
+                    b[off + l + n * k] = b_l[l + 128 * k];
+                }
+        }
+    }
+    return 0;
+}
+
 }  // extern "C"

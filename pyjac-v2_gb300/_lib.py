@@ -58,6 +58,12 @@ SIGNATURES = [
     ("pjg_profile_end", ctypes.c_int, [ctypes.POINTER(ctypes.c_int64),
                                        ctypes.POINTER(ctypes.c_double)]),
     ("pjg_math_exp", ctypes.c_int, [_VP, _VP, ctypes.c_int64, _VP]),
+    ("pjg_read_initial_conditions", ctypes.c_int,
+     [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_char, _VP, _VP]),
+    ("pjg_write_initial_conditions", ctypes.c_int,
+     [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_char, _VP, _VP]),
+    ("pjg_chem_utils", ctypes.c_int,
+     [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, _VP, _VP, _VP, _VP, _VP]),
 ]
 
 

@@ -116,6 +116,25 @@ class Evaluator(DeviceMechanism):
             raise ValueError("phi must hold %d x %d values" % (n, self.nn))
         return n, torch.cuda.current_stream(param.device).cuda_stream
 
+    def chem_utils(self, phi, order="C", conp=True):
+        """Species thermo at each state's (guarded) temperature: (cp, h, b), or
+        (cv, u, b) when not conp; each (N, Ns) for order 'C', (Ns, N) for 'F'."""
+        import torch
+        if not (isinstance(phi, torch.Tensor) and phi.is_cuda and phi.dtype == torch.float64
+                and phi.is_contiguous()):
+            raise TypeError("expected a contiguous CUDA float64 tensor")
+        if phi.numel() % self.nn:
+            raise ValueError("phi must hold N x %d values" % self.nn)
+        n = phi.numel() // self.nn
+        ns = self.nn - 1
+        shape = (n, ns) if order == "C" else (ns, n)
+        out = [torch.empty(shape, dtype=torch.float64, device=phi.device) for _ in range(3)]
+        st = torch.cuda.current_stream(phi.device).cuda_stream
+        _lib.check("pjg_chem_utils", self._lib.pjg_chem_utils(
+            self.handle, n, _order(order), int(bool(conp)), phi.data_ptr(), out[0].data_ptr(),
+            out[1].data_ptr(), out[2].data_ptr(), st))
+        return tuple(out)
+
     def species_rates(self, param, phi, order="C", conp=True, out=None):
         import torch
         n, st = self._prep(param, phi, order)
@@ -259,5 +278,45 @@ def pywrap(mech, order="C", conp=True, jac_format="full"):
                  _dev_mech=staticmethod(dev_mech))
     jk = type("PyJacobianKernel", (_KernelBase,), dict(attrs, _kind=KIND_JAC))
     rk = type("PySpecies_RatesKernel", (_KernelBase,), dict(attrs, _kind=KIND_RATES))
-    return types.SimpleNamespace(PyJacobianKernel=jk, PySpecies_RatesKernel=rk, mechanism=mech,
-                                 order=order, conp=bool(conp), jac_format=jac_format)
+    ck = type("PyChem_UtilsKernel", (_ChemUtilsKernel,), attrs)
+    return types.SimpleNamespace(PyJacobianKernel=jk, PySpecies_RatesKernel=rk,
+                                 PyChem_UtilsKernel=ck, mechanism=mech, order=order,
+                                 conp=bool(conp), jac_format=jac_format)
+
+
+class _ChemUtilsKernel(object):
+    """The chem_utils kernel type of the generated module: call(phi, cp, h, b)
+    fills cp, h, b (cv, u, b when not conp), each Ns values per state in the
+    kernel's order, from host arrays."""
+
+    def __init__(self, problem_size, work_size, do_not_compile=False, **kwargs):
+        kwargs.pop("testing_only_skip_compilation", None)
+        if kwargs:
+            raise TypeError("unexpected keyword arguments %s" % sorted(kwargs))
+        self._ev = Evaluator(self._mech)
+        self.resize(problem_size, work_size)
+
+    def resize(self, problem_size, work_size, do_not_compile=False):
+        self.problem_size = int(problem_size)
+        self.work_size = int(work_size)
+
+    def num_species(self):
+        return self._mech.n_species
+
+    def order(self):
+        return self._order
+
+    def __call__(self, phi, cp, h, b):
+        import torch
+        n, ns = self.problem_size, self._mech.n_species
+        for a, sz, name in ((phi, n * (ns + 1), "phi"), (cp, n * ns, "cp"), (h, n * ns, "h"),
+                            (b, n * ns, "b")):
+            if not isinstance(a, np.ndarray) or a.dtype != np.float64 or a.size != sz:
+                raise ValueError("%s must be a float64 numpy array of %d values" % (name, sz))
+        x = torch.from_numpy(np.ascontiguousarray(phi).reshape(-1)).cuda()
+        outs = self._ev.chem_utils(x, order=self._order, conp=self._conp)
+        for host, dev in zip((cp, h, b), outs):
+            host.reshape(-1)[:] = dev.reshape(-1).cpu().numpy()
+
+    def close(self):
+        pass

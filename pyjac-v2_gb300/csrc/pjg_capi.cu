@@ -72,7 +72,7 @@ struct SlotTables {
 }  // namespace
 
 struct pjg_mech {
-    int ns = 0, nr = 0, nn = 0, need_logP = 0, nnz = 0;
+    int ns = 0, nr = 0, nn = 0, need_logP = 0, nnz = 0, jac_approx = 0;
     int device = 0;
     PjgRxn* rxn = nullptr;
     double* sp = nullptr;
@@ -276,6 +276,7 @@ void fill_common(const pjg_mech* m, EvalArgs& a)
     a.ns = m->ns;
     a.nr = m->nr;
     a.need_logP = m->need_logP;
+    a.jac_approx = m->jac_approx;
 }
 
 // Per-state bytes of working arrays one evaluation needs.  The Jacobian
@@ -478,6 +479,22 @@ int pjg_fp64_peak(double* tflops)
     return 0;
 }
 
+int pjg_chem_utils(pjg_mech* m, int64_t n, char order, int conp, const double* phi, double* cp,
+                   double* h, double* b, void* stream)
+{
+    if (!m) return fail(PJG_ERR_ARG, "null mechanism");
+    if (n < 0) return fail(PJG_ERR_ARG, "negative problem size");
+    if (order != 'C' && order != 'F') return fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
+    if (n == 0) return 0;
+    if (!phi || !cp || !h || !b) return fail(PJG_ERR_ARG, "null array");
+    const bool F = order == 'F';
+    if (pjg_launch_chem_utils(m->sp, m->ns, n, conp, phi, F ? 1 : m->nn, cp, h, b, F ? 1 : m->ns,
+                              F ? n : 1, stream))
+        return fail(PJG_ERR_CUDA, "chem_utils launch failed");
+    g_launches.fetch_add(1);
+    return 0;
+}
+
 int pjg_math_exp(const double* x, double* y, int64_t n, void* stream)
 {
     if (n < 0) return fail(PJG_ERR_ARG, "negative size");
@@ -542,6 +559,7 @@ int pjg_mech_create(const pjg_tables* tb, pjg_mech** out)
     m->nr = tb->nr;
     m->nn = NN;
     m->need_logP = tb->flags & 1;
+    m->jac_approx = (tb->flags >> 1) & 1;
     m->nnz = tb->nnz;
     cudaGetDevice(&m->device);
     const PjgRxn* r = (const PjgRxn*)tb->rxn;

@@ -212,14 +212,14 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
                     if (jb >= nsp) break;
                     if (ent_spec(ent[jb]) != last) accum(nsrow, ent_spec(ent[jb]), wc * g[jb]);
                 }
-                if (hasns) vNS = fma(wc, gns, vNS);
+                if (hasns && !a.jac_approx) vNS = fma(wc, gns, vNS);
                 if (thd) {
                     const double wx = w * X;
                     for (int l = 0; l < thd_cnt; ++l) {
                         const int j = __ldg(a.thd_spec + thd_off + l);
                         if (j != last) accum(nsrow, j, __ldg(a.thd_coef + thd_off + l) * wx);
                     }
-                    if (nslist) vNS = fma(cns, wx, vNS);
+                    if (nslist && !a.jac_approx) vNS = fma(cns, wx, vNS);
                 }
                 vout0 = fma(w, d0, vout0);
                 vout1 = fma(w, d1, vout1);
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
                 }
                 if (nslist) nsacc = fma(cns, X, nsacc);
             }
-            if (hasns || (thd && nslist)) accum(nsrow, k, nux(nuk, nsacc));
+            if ((hasns || (thd && nslist)) && !a.jac_approx) accum(nsrow, k, nux(nuk, nsacc));
         }
     }
 
@@ -419,7 +419,41 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     acc[(int64_t)a.s11 * ld] = J11;
 }
 
+// Species thermo of the chem_utils kernel type (rate_subs.py write_chem_utils
+// :3391-3444, polyfit_kernel_gen :3281-3388): at the guarded temperature,
+// cp (cv), h (u) and the Gibbs function b of every species.  Entry (s, k) of
+// each output at out[s * out_ss + k * out_sk].
+__global__ void __launch_bounds__(PJG_BLOCK) chem_utils_kernel(const double* __restrict__ sp, int ns,
+                                                               int64_t n, int conp,
+                                                               const double* __restrict__ phi,
+                                                               int64_t phi_ss, double* cp, double* h,
+                                                               double* b, int64_t out_ss,
+                                                               int64_t out_sk)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const double Tc = fmin(10000.0, fmax(100.0, phi[s * phi_ss]));
+    const double logT = log(Tc), Tinv = 1.0 / Tc;
+    for (int k = 0; k < ns; ++k) {
+        const Thermo t = thermo<false>(sp + (int64_t)k * PJG_SP_DOUBLES, Tc, logT, Tinv, conp);
+        const int64_t o = s * out_ss + (int64_t)k * out_sk;
+        cp[o] = t.cp;
+        h[o] = t.h;
+        b[o] = t.b;
+    }
+}
+
 }  // namespace
+
+int pjg_launch_chem_utils(const double* sp, int ns, int64_t n, int conp, const double* phi,
+                          int64_t phi_ss, double* cp, double* h, double* b, int64_t out_ss,
+                          int64_t out_sk, void* stream)
+{
+    if (n <= 0) return 0;
+    chem_utils_kernel<<<(unsigned)((n + PJG_BLOCK - 1) / PJG_BLOCK), PJG_BLOCK, 0, (cudaStream_t)stream>>>(
+        sp, ns, n, conp, phi, phi_ss, cp, h, b, out_ss, out_sk);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
 
 namespace {
 

@@ -30,6 +30,7 @@ struct EvalArgs {
     const double* aux;
     int ns, nr;
     int need_logP;
+    int jac_approx;  // 'approximate' Jacobian type: no bath-gas terms in the species columns
     // states
     int64_t n;  // states in this launch
     int conp;
@@ -67,5 +68,8 @@ int pjg_eval_blocks_per_sm(int kind);
 int pjg_launch_zero(double* acc, int64_t ld, int64_t n, int nslot, void* stream);
 int pjg_fp64_probe(int blocks, int threads, int iters, double* out, void* stream);
 int pjg_launch_fexp(const double* x, double* y, int64_t n, void* stream);
+int pjg_launch_chem_utils(const double* sp, int ns, int64_t n, int conp, const double* phi,
+                          int64_t phi_ss, double* cp, double* h, double* b, int64_t out_ss,
+                          int64_t out_sk, void* stream);
 int pjg_launch_transpose(const double* src, int64_t ld, int64_t n, int nslot, double* dst,
                          void* stream);

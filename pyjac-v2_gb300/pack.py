@@ -206,7 +206,9 @@ class PackedTables(object):
         self.n_thd = len(thd_spec)
         self.aux = np.asarray(aux if aux else [0.0], dtype=np.float64)
         self.n_aux = len(aux)
-        self.flags = 1 if need_logP else 0
+        # bit 0: PLOG / Chebyshev present (ln P needed); bit 1: the 'approximate'
+        # Jacobian type (no bath-gas terms in the species columns)
+        self.flags = (1 if need_logP else 0) | (2 if getattr(mech, "jac_type", "exact") == "approximate" else 0)
         ji = v["jac_inds"]
         self.crs_row_ptr = np.ascontiguousarray(ji["crs"]["row_ptr"], dtype=np.int32)
         self.crs_col_ind = np.ascontiguousarray(ji["crs"]["col_ind"], dtype=np.int32)

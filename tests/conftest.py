@@ -39,7 +39,16 @@ MECH_FILES = {
 _cache = {}
 
 
-def load_mech(name):
+def load_mech(name, jac_type="exact"):
+    """Mechanism by name; jac_type 'approximate' gives the tables of that
+    Jacobian type (pattern without the bath-gas full rows)."""
+    if jac_type != "exact":
+        key = (name, jac_type)
+        if key not in _cache:
+            base = load_mech(name)
+            _cache[key] = pkg("mech").Mechanism(base.elements, base.species, base.reactions,
+                                                base.rate_spec, jac_type, source=base.source)
+        return _cache[key]
     if name not in _cache:
         if name == "synthetic500":
             # the 500-species, 2,500-reaction benchmark mechanism (seed 0),

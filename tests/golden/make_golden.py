@@ -13,7 +13,11 @@ Writes
 * ``ref_<mech>.npz`` for h2o2 and gri30: seeded states and the outputs of the
   reference's shipped generated kernels (examples/opencl/{h2o2,ch4},
   shim-compiled by oracle/build_ref.py): dphi and the Jacobian in the shipped
-  format (dense F for H2/O2, sparse CCS for GRI-30), F order, conp;
+  format (dense F for H2/O2, sparse CCS for GRI-30), F order, conp; and the
+  shipped chem_utils outputs (cp, h, b) over a temperature sweep through both
+  NASA ranges and beyond the 100 K / 10,000 K guards;
+* ``jacapprox_<mech>.npz``: the reference front end's Jacobian index arrays
+  for the 'approximate' Jacobian type (same four mechanisms);
 * ``synthetic_small.inp``: the seeded all-forms synthetic mechanism.
 """
 import argparse
@@ -75,6 +79,12 @@ def main():
         flat["species_names"] = np.array([s.name for s in specs])
         flat["reaction_strings"] = np.array([r.rxn_str for r in reacs])
         np.savez_compressed(os.path.join(HERE, "tables_%s.npz" % name), **flat)
+        # the 'approximate' Jacobian type's index arrays (create_jacobian.py:186-190)
+        _, _, aval = rf.reference_tables(os.path.join(ROOT, mech),
+                                         os.path.join(ROOT, therm) if therm else None,
+                                         jac_type="approximate", reference=a.reference)
+        np.savez_compressed(os.path.join(HERE, "jacapprox_%s.npz" % name),
+                            **flatten(aval["jac_inds"]))
     build_ref = importlib.import_module("build_ref")
     build_ref.build(a.reference, quiet=True)
     orc = importlib.import_module("oracle")
@@ -85,8 +95,14 @@ def main():
         phiF = np.ascontiguousarray(phi.T)
         dphi = ref.species_rates_F(P, phiF, nthreads=1)
         jac = ref.jacobian_F(P, phiF, nthreads=1)
+        # species thermo (chem_utils) over a temperature sweep through both
+        # NASA ranges and beyond the 100 K / 10,000 K guard
+        cu_phi = np.repeat(phi[:1], 256, axis=0)
+        cu_phi[:, 0] = np.linspace(50.0, 12000.0, 256)
+        cp, h, b = ref.chem_utils_F(np.ascontiguousarray(cu_phi.T), nthreads=1)
         np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % name), P=P, phi=phi,
-                            dphi_F=dphi, jac_F=jac)
+                            dphi_F=dphi, jac_F=jac, cu_phi=cu_phi, cu_cp_F=cp, cu_h_F=h,
+                            cu_b_F=b)
     print("golden fixtures written to", HERE)
 
 

@@ -252,3 +252,64 @@ def test_synthetic500_rates_and_sparse_jacobian(cuda_device, order):
     assert row_rel_err(J, np.where(mask[None], Jref, 0.0)) < RTOL_JAC
     # the pattern holds every non-zero of the analytical Jacobian
     assert (np.abs(np.where(mask[None], 0.0, Jref)) <= 1e-12 * np.abs(Jref).max()).all()
+
+
+@pytest.mark.parametrize("name", MECHS)
+@pytest.mark.parametrize("conp", [True, False])
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_chem_utils(cuda_device, name, conp, order):
+    """Species thermo (the chem_utils kernel type) against the oracle, over
+    temperatures through both NASA ranges and beyond the guards.  h and b
+    cross zero along the sweep, so the error is measured against each
+    species' largest magnitude (the kernels use precomputed polynomial
+    quotients, the oracle divides: last-ulp differences)."""
+    mech = load_mech(name)
+    n = 300
+    P, phi = states(name, n, 19, conp)
+    phi = phi.copy()
+    phi[:, 0] = np.linspace(50.0, 12000.0, n)
+    ref = oracle_mod().Oracle(mech).chem_utils(phi, conp=conp)
+    x = phi if order == "C" else phi.T
+    got = evaluator(name).chem_utils(to_dev(x, cuda_device), order=order, conp=conp)
+    for g, r in zip(got, ref):
+        g = g.cpu().numpy()
+        g = g if order == "C" else g.T
+        scale = np.abs(r).max(axis=0, keepdims=True)
+        assert np.max(np.abs(g - r) / scale) < 1e-13
+
+
+def test_pywrap_chem_utils_kernel(cuda_device):
+    mech = load_mech("gri30")
+    n = 129
+    P, phi = states("gri30", n, 20, True)
+    mod = pkg("api").pywrap(mech, order="F", conp=True)
+    ck = mod.PyChem_UtilsKernel(n, 1)
+    x = np.ascontiguousarray(phi.T)
+    cp, h, b = (np.zeros(n * mech.n_species) for _ in range(3))
+    ck(x, cp, h, b)
+    ref = oracle_mod().Oracle(mech).chem_utils(phi)
+    for got, r in zip((cp, h, b), ref):
+        scale = np.abs(r).max(axis=0, keepdims=True)
+        assert np.max(np.abs(got.reshape(mech.n_species, n).T - r) / scale) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30", "testmech", "synthetic_small"])
+@pytest.mark.parametrize("order", ["C", "F"])
+@pytest.mark.parametrize("fmt", ["full", "sparse"])
+def test_approximate_jacobian(cuda_device, name, order, fmt):
+    """The 'approximate' Jacobian type (tables flag bit 1): its own pattern,
+    bit-exact index arrays, and values equal to the oracle's approximate
+    Jacobian."""
+    mech = load_mech(name, jac_type="approximate")
+    n = 200
+    P, phi = states(name, n, 21, True)
+    Jref = oracle_mod().Oracle(mech).jacobian(P, phi)
+    ev = pkg("api").Evaluator(mech)
+    ptr, ind = ev.jacobian_indices(order)
+    eptr, eind = mech.pattern(order)
+    assert np.array_equal(ptr, eptr) and np.array_equal(ind, eind)
+    x = phi if order == "C" else phi.T
+    out = ev.jacobian(to_dev(P, cuda_device), to_dev(x, cuda_device), order=order,
+                      jac_format=fmt).cpu().numpy()
+    assert np.isfinite(out).all()
+    assert row_rel_err(_dense_from(out, order, fmt, mech, ev, n), Jref) < RTOL_JAC

@@ -85,3 +85,39 @@ def test_oracle_guards_out_of_range_states():
     assert np.isfinite(d[:3]).all()
     J = o.jacobian(P, phi[:3])
     assert np.isfinite(J).all()
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30"])
+def test_oracle_chem_utils_matches_shipped_reference(name):
+    """Species thermo (the chem_utils kernel type: cp, h, b at the guarded T)
+    against the shipped chem_utils kernel over a 50 K - 12,000 K sweep."""
+    g = np.load(os.path.join(GOLDEN, "ref_%s.npz" % name))
+    o = oracle_mod().Oracle(load_mech(name))
+    for got, ref in zip(o.chem_utils(g["cu_phi"]), (g["cu_cp_F"], g["cu_h_F"], g["cu_b_F"])):
+        ref = ref.T
+        assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30", "testmech", "synthetic_small"])
+def test_oracle_approximate_jacobian_drops_only_bath_gas_terms(name):
+    """The 'approximate' type omits d n_Ns / d n_j in the reaction-rate
+    derivatives (create_jacobian.py:3578-3582, :4187-4191): in every species
+    row the exact and approximate Jacobians differ by the same amount in all
+    species columns, and not at all in the T and E columns."""
+    exact, approx = load_mech(name), load_mech(name, jac_type="approximate")
+    P, phi = bath_rich_states(exact, 32, 5)
+    Je = oracle_mod().Oracle(exact).jacobian(P, phi)
+    Ja = oracle_mod().Oracle(approx).jacobian(P, phi)
+    d = Je[:, 2:, :] - Ja[:, 2:, :]
+    scale = np.abs(Je[:, 2:, :]).max(axis=2, keepdims=True) + 1e-300
+    assert (np.abs(d[:, :, :2]) / scale).max() < 1e-13
+    spread = d[:, :, 2:].max(axis=2) - d[:, :, 2:].min(axis=2)
+    assert (spread / scale[:, :, 0]).max() < 1e-11
+    # the approximate pattern holds every non-zero of the approximate Jacobian
+    ptr, ind = approx.pattern("C")
+    mask = np.zeros((approx.nn, approx.nn), dtype=bool)
+    for r in range(approx.nn):
+        mask[r, ind[ptr[r]:ptr[r + 1]]] = True
+    assert (Ja[:, ~mask] == 0).all()
+    if name in ("h2o2", "gri30"):  # mechanisms with bath-gas reactions
+        assert np.abs(d[:, :, 2:]).max() > 0
