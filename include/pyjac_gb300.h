@@ -168,6 +168,30 @@ int pjg_mlp_linear(const void* X, int64_t ldx, const void* W, int64_t ldw, int64
 int pjg_mlp_wgrad(const void* A, int64_t lda, const void* B, int64_t ldb, int Mo, int No,
                   int64_t Kb, float* C, int64_t ldc, void* stream);
 int pjg_mlp_status(int clear);
+/* The whole surrogate forward pass in one launch: Y [M x 64] (FP32) =
+ * L4(SiLU(L3(SiLU(L2(SiLU(L1(SiLU(L0(X)))))))) for X [M x 64] BF16, where
+ * Ll(a) = a Wl^T + bl with W0 [256 x 64], W1..W3 [256 x 256], W4 [64 x 256].
+ * W[l] points at Wl in BF16, packed in 8-row x 16-byte core matrices, row
+ * group major: byte ((n / 8) * (K / 8) + k / 8) * 128 + (n % 8) * 16 + (k % 8) * 2
+ * holds W[n][k].  b[l] are FP32 biases.  Activations stay on chip between the
+ * layers.  No reference counterpart (the learned wdot surrogate). */
+int pjg_mlp_forward(const void* X, int64_t ldx, int64_t M, const void* const* W,
+                    const float* const* b, float* Y, int64_t ldy, void* stream);
+/* Surrogate input and output stages on device arrays (states in order 'C',
+ * constant pressure).  Features: X [n x 64] BF16 = ((T - 1500) / 400,
+ * (ln P - mu_P) / sd_P, (log10 max(c_k, floor) - mu_k) / sd_k ..., 0 ...),
+ * c_k = max(n_k, 0) / V; stats = (mu_P, sd_P, mu[nn - 2], sd[nn - 2]).
+ * Outputs: from the network outputs Y [n x 64] FP32, the rates
+ * y_j = sinh(Y_j z_sd_j + z_mu_j) s_j of (dT/dt, dn_k/dt) and the
+ * extra-variable rate recomputed from them as the FP64 path does, written to
+ * dphi [n x nn]; lerr[n] = Y[s][err_col] (the predicted log10 error);
+ * stats = (z_mu[nn - 1], z_sd[nn - 1], s[nn - 1], 1 - W_k / W_ns [nn - 2]).
+ * No reference counterpart (the learned wdot surrogate). */
+int pjg_surrogate_features(int64_t n, int32_t nn, const double* phi, const double* param,
+                           const double* stats, void* X, double floor_c, void* stream);
+int pjg_surrogate_outputs(int64_t n, int32_t nn, const float* Y, const double* phi,
+                          const double* param, const double* stats, int32_t err_col, double* dphi,
+                          float* lerr, void* stream);
 
 /* Binary initial-condition files: the reference's read_initial_conditions
  * (pyjac/kernel_utils/common/read_initial_conditions.cpp.in:30-116).  One

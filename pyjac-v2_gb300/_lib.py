@@ -52,6 +52,13 @@ SIGNATURES = [
      [_VP, ctypes.c_int64, _VP, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int64, _VP,
       ctypes.c_int64, _VP]),
     ("pjg_mlp_status", ctypes.c_int, [ctypes.c_int]),
+    ("pjg_surrogate_features", ctypes.c_int,
+     [ctypes.c_int64, ctypes.c_int32, _VP, _VP, _VP, _VP, ctypes.c_double, _VP]),
+    ("pjg_surrogate_outputs", ctypes.c_int,
+     [ctypes.c_int64, ctypes.c_int32, _VP, _VP, _VP, _VP, ctypes.c_int32, _VP, _VP, _VP]),
+    ("pjg_mlp_forward", ctypes.c_int,
+     [_VP, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(_VP), ctypes.POINTER(_VP), _VP,
+      ctypes.c_int64, _VP]),
     ("pjg_launch_count", ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
     ("pjg_fp64_peak", ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     ("pjg_profile_begin", ctypes.c_int, []),

@@ -452,6 +452,45 @@ int pjg_mlp_wgrad(const void* A, int64_t lda, const void* B, int64_t ldb, int Mo
 
 int pjg_mlp_status(int clear) { return mlp_error_flag(clear); }
 
+int pjg_surrogate_features(int64_t n, int32_t nn, const double* phi, const double* param,
+                           const double* stats, void* X, double floor_c, void* stream)
+{
+    if (n < 0 || (n && (!phi || !param || !stats || !X)))
+        return fail(PJG_ERR_ARG, "pjg_surrogate_features: bad arguments");
+    const int rc = surr_launch_features(n, nn, phi, param, stats, X, (float)floor_c, stream);
+    if (rc == -1) return fail(PJG_ERR_ARG, "pjg_surrogate_features: 3 <= nn <= 64, X 16-byte aligned");
+    if (rc) return fail(PJG_ERR_CUDA, "pjg_surrogate_features launch failed");
+    if (n > 0) g_launches.fetch_add(1);
+    return 0;
+}
+
+int pjg_surrogate_outputs(int64_t n, int32_t nn, const float* Y, const double* phi,
+                          const double* param, const double* stats, int32_t err_col, double* dphi,
+                          float* lerr, void* stream)
+{
+    if (n < 0 || (n && (!Y || !phi || !param || !stats || !dphi || !lerr)))
+        return fail(PJG_ERR_ARG, "pjg_surrogate_outputs: bad arguments");
+    const int rc = surr_launch_outputs(n, nn, Y, phi, param, stats, err_col, dphi, lerr, stream);
+    if (rc == -1) return fail(PJG_ERR_ARG, "pjg_surrogate_outputs: 3 <= nn <= 65, 0 <= err_col < 64");
+    if (rc) return fail(PJG_ERR_CUDA, "pjg_surrogate_outputs launch failed");
+    if (n > 0) g_launches.fetch_add(1);
+    return 0;
+}
+
+int pjg_mlp_forward(const void* X, int64_t ldx, int64_t M, const void* const* W,
+                    const float* const* b, float* Y, int64_t ldy, void* stream)
+{
+    if (M < 0 || !W || !b) return fail(PJG_ERR_ARG, "pjg_mlp_forward: bad arguments");
+    int rc = mlp_launch_fused(X, ldx, M, W, b, Y, ldy, stream);
+    if (rc == -1)
+        return fail(PJG_ERR_ARG, "pjg_mlp_forward: operands must be 16-byte aligned, ldx %% 8, "
+                                 "ldy %% 4, ldx and ldy >= 64");
+    if (rc) return fail(PJG_ERR_CUDA, "pjg_mlp_forward launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+    if (M > 0) g_launches.fetch_add(1);
+    return 0;
+}
+
 int pjg_fp64_peak(double* tflops)
 {
     if (!tflops) return fail(PJG_ERR_ARG, "null argument");

@@ -8,4 +8,10 @@ int mlp_launch_rows(const void* A, int64_t lda, const void* B, int64_t ldb, int6
                  float* colsum, void* stream);
 int mlp_launch_wgrad(const void* A, int64_t lda, const void* B, int64_t ldb, int Mo, int No, int64_t Kb,
                   float* C, int64_t ldc, void* stream);
+int mlp_launch_fused(const void* X, int64_t ldx, int64_t M, const void* const* W,
+                     const float* const* b, float* Y, int64_t ldy, void* stream);
+int surr_launch_features(int64_t n, int nn, const double* phi, const double* param,
+                         const double* st, void* X, float floor_c, void* stream);
+int surr_launch_outputs(int64_t n, int nn, const float* Y, const double* phi, const double* param,
+                        const double* st, int err_col, double* dphi, float* lerr, void* stream);
 int mlp_error_flag(int clear);

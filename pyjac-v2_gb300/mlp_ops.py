@@ -5,6 +5,8 @@ biases, gradients and outputs.  Calls are asynchronous on the current torch
 stream.  There is no fallback: a missing library or an unsupported shape
 raises.
 """
+import ctypes
+
 import torch
 
 from . import _lib
@@ -61,6 +63,29 @@ def wgrad(A, B, C):
     _lib.check("pjg_mlp_wgrad", lib.pjg_mlp_wgrad(
         _ptr(A), _ld(A), _ptr(B), _ld(B), Mo, No, Kb, _ptr(C), _ld(C), st))
     return C
+
+
+def pack_core(W):
+    """BF16 [N, K] -> the core-matrix layout of pjg_mlp_forward (N, K multiples of 8):
+    8-row x 16-byte blocks, row-group major, then K."""
+    N, K = W.shape
+    return W.to(torch.bfloat16).reshape(N // 8, 8, K // 8, 8).permute(0, 2, 1, 3).contiguous()
+
+
+def forward_fused(X, Wp, b, Y=None):
+    """The whole network in one tcgen05 launch: X [M, 64] bf16, Wp the five
+    packed weights (pack_core), b the five FP32 biases -> Y [M, 64] fp32."""
+    lib = _lib.load()
+    _check(X, torch.bfloat16, "X")
+    M = X.shape[0]
+    if Y is None:
+        Y = torch.empty(M, 64, dtype=torch.float32, device=X.device)
+    W = (ctypes.c_void_p * 5)(*[w.data_ptr() for w in Wp])
+    B = (ctypes.c_void_p * 5)(*[x.data_ptr() for x in b])
+    st = torch.cuda.current_stream(X.device).cuda_stream
+    _lib.check("pjg_mlp_forward", lib.pjg_mlp_forward(X.data_ptr(), X.stride(0), M, W, B,
+                                                      Y.data_ptr(), Y.stride(0), st))
+    return Y
 
 
 def status(clear=True):

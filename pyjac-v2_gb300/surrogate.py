@@ -24,7 +24,7 @@ import time
 import numpy as np
 import torch
 
-from . import api, mlp_ops
+from . import _lib, api, mlp_ops
 from .mech.elements import RU
 
 HID = 256
@@ -63,6 +63,7 @@ class MLP(object):
     def refresh(self):
         self.Wb = [w.to(torch.bfloat16).contiguous() for w in self.W]
         self.Wtb = [w.t().contiguous().to(torch.bfloat16) for w in self.W]
+        self.Wp = [mlp_ops.pack_core(w) for w in self.Wb]  # operands of the fused forward
 
     def _get(self, key, shape, dtype):
         b = self._buf.get(key)
@@ -87,6 +88,11 @@ class MLP(object):
         Y = out if out is not None else self._get(("Y", keep), (M, NOUT_P), torch.float32)
         mlp_ops.linear(a, self.Wb[4], bias=self.b[4], Y32=Y)
         return Y
+
+    def infer(self, X, out=None):
+        """Inference: the whole network in one fused tcgen05 launch (activations
+        stay on chip); same result as forward(X)."""
+        return mlp_ops.forward_fused(X, self.Wp, self.b, Y=out)
 
     def backward(self, XT, dY):
         """Weight and bias gradients for the last forward(keep=True); XT = X^T [64, M]."""
@@ -321,17 +327,45 @@ class Surrogate(object):
         return hist
 
     # ----------------------------------------------------------- inference
+    def _stage_stats(self):
+        """Device copies of the statistics the fused input / output stages read."""
+        key = id(self.stats)
+        if getattr(self, "_stage_key", None) != key:
+            st = self.stats
+            self._feat_stats = torch.cat([st["lnP_mu"].reshape(1), st["lnP_sd"].reshape(1),
+                                          st["lc_mu"], st["lc_sd"]]).double().contiguous()
+            self._out_stats = torch.cat([st["z_mu"], st["z_sd"], st["s"],
+                                         self.omw]).double().contiguous()
+            self._stage_key = key
+        return self._feat_stats, self._out_stats
+
+    def predict(self, param, phi):
+        """Surrogate dphi (n, NN) and the predicted log10 relative errors, no
+        fallback: three launches (features, the fused network, outputs)."""
+        fst, ost = self._stage_stats()
+        n, nn = phi.shape
+        lib = _lib.load()
+        st = torch.cuda.current_stream(phi.device).cuda_stream
+        X = torch.empty(n, NIN_P, dtype=torch.bfloat16, device=phi.device)
+        _lib.check("pjg_surrogate_features", lib.pjg_surrogate_features(
+            n, nn, phi.data_ptr(), param.data_ptr(), fst.data_ptr(), X.data_ptr(), FEAT_FLOOR, st))
+        Y = self.net.infer(X)
+        out = torch.empty_like(phi)
+        lerr = torch.empty(n, dtype=torch.float32, device=phi.device)
+        _lib.check("pjg_surrogate_outputs", lib.pjg_surrogate_outputs(
+            n, nn, Y.data_ptr(), phi.data_ptr(), param.data_ptr(), ost.data_ptr(), ERR,
+            out.data_ptr(), lerr.data_ptr(), st))
+        return out, lerr, X
+
     def predict_raw(self, param, phi, out_buf=None):
-        """Network rates (53) and log10 error estimates, no fallback."""
-        X = self.features(param, phi).to(torch.bfloat16).contiguous()
-        Y = self.net.forward(X, out=out_buf)
-        y = self.untransform(Y[:, :NOUT])
-        return y, Y[:, ERR], X
+        """Network rates (53: dT/dt and the species rates) and log10 error
+        estimates, no fallback."""
+        out, lerr, X = self.predict(param, phi)
+        return torch.cat([out[:, :1], out[:, 2:]], dim=1), lerr, X
 
     def species_rates(self, param, phi, tol=1e-3, margin=0.5, return_info=False):
         """dphi (n, NN) with the surrogate where trusted, FP64 elsewhere."""
-        y, lerr, X = self.predict_raw(param, phi)
-        out = self.assemble(param, phi, y)
+        out, lerr, X = self.predict(param, phi)
         box_lo, box_hi = self.stats["box_lo"], self.stats["box_hi"]
         f = X[:, :2].float()
         ood = ((f < box_lo - 1e-3) | (f > box_hi + 1e-3)).any(dim=1)

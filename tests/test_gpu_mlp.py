@@ -71,3 +71,25 @@ def test_wgrad_matches_torch(cuda_device, Mo, No, Kb):
     ref = A.float() @ B.float().t()
     assert ops.status() == 0
     assert rel(C, ref) < 1e-5
+
+
+@pytest.mark.parametrize("M", [1, 127, 128, 4097, 300000])
+def test_fused_forward_matches_layer_by_layer(cuda_device, M):
+    """pjg_mlp_forward (all five layers in one launch, activations on chip,
+    weights streamed by bulk copies) equals the layer-by-layer tcgen05 forward:
+    the same BF16 roundings at the same points."""
+    import torch
+    sg = pkg("surrogate")
+    net = sg.MLP(cuda_device, seed=7)
+    g = torch.Generator(device=cuda_device).manual_seed(3)
+    for b in net.b:
+        b.copy_(0.1 * torch.randn(b.shape, generator=g, device=cuda_device))
+    net.refresh()
+    X = torch.randn(M, 64, generator=g, device=cuda_device).to(torch.bfloat16)
+    X[:, 54:] = 0
+    ref = net.forward(X.contiguous())
+    got = net.infer(X.contiguous())
+    torch.cuda.synchronize()
+    assert pkg("mlp_ops").status() == 0
+    err = ((got - ref).abs() / (ref.abs() + 1e-2)).max().item()
+    assert err < 1e-3, err

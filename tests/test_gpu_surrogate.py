@@ -97,3 +97,24 @@ def test_surrogate_inference_faster_than_fp64_kernel(cuda_device):
     torch.cuda.synchronize()
     t_fp64 = time.perf_counter() - t0
     assert t_net < t_fp64, (t_net, t_fp64)
+
+
+def test_fused_input_and_output_stages_match_torch(cuda_device):
+    """The inference stages in CUDA (features with FP32 logarithms, the fused
+    network, outputs with FP32 sinh) against the torch formulation of the same
+    transforms (FP64): features within one BF16 rounding, rates within 1e-5."""
+    import torch
+    sg = pkg("surrogate")
+    mech = load_mech("gri30")
+    s = sg.Surrogate(mech, device=cuda_device, seed=2)
+    data = s.make_data(20000, seed=5, sobolev=False)
+    P, phi = data["P"], data["phi"]
+    out, lerr, X = s.predict(P, phi)
+    Xt = s.features(P, phi).to(torch.bfloat16)
+    ulp = (X.float() - Xt.float()).abs() / (Xt.float().abs() + 1e-3)
+    assert ulp.max().item() <= 2.0 ** -7
+    Y = s.net.forward(X.contiguous())
+    ref = s.assemble(P, phi, s.untransform(Y[:, :sg.NOUT]))
+    scale = ref.abs().max(dim=0).values + 1e-300
+    assert ((out - ref).abs() / scale).max().item() < 1e-5
+    assert torch.equal(lerr, Y[:, sg.ERR])
