@@ -356,10 +356,7 @@ def main():
     n_eval, eval_ms = lib.profile_end()
     launches = lib.launch_count() - launches0
     ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = pkg("shard").max_over_ranks(ms, device=dev)  # the slowest rank
     clk = clocks.stop()
     ms_step = ms / args.steps
     value = world * n * args.steps / (ms * 1e-3)
