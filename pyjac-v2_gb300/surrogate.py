@@ -143,8 +143,14 @@ class MLP(object):
 class Surrogate(object):
     """The learned wdot surrogate of one mechanism (constant pressure, 'C' order)."""
 
-    def __init__(self, mech, device="cuda", seed=0, evaluator=None):
+    def __init__(self, mech, device="cuda", seed=0, evaluator=None, target_scale=1.0):
+        """target_scale: the rates are mapped through asinh(y / (target_scale * rms));
+        small values make the targets logarithmic, larger ones keep the
+        dominant rates of a state closer to linear.  Measured on GRI-Mech 3.0
+        (2M training states, 8 epochs), median / p90 per-state relative error:
+        2.8 / 71 at 1e-4, 0.42 / 1.9 at 1e-2, 0.39 / 0.76 at 1."""
         self.mech = mech
+        self.target_scale = float(target_scale)
         self.device = torch.device(device)
         self.ev = evaluator if evaluator is not None else api.Evaluator(mech)
         self.net = MLP(self.device, seed)
@@ -261,7 +267,7 @@ class Surrogate(object):
         y = torch.cat([dphi[:, :1], dphi[:, 2:]], dim=1)
         rms = y.pow(2).mean(0).sqrt().clamp_min(1e-30)
         s["y_rms"] = rms
-        s["s"] = 1e-4 * rms
+        s["s"] = self.target_scale * rms
         z = torch.asinh(y / s["s"])
         s["z_mu"], s["z_sd"] = z.mean(0), z.std(0).clamp_min(1e-6)
         s["box_lo"] = torch.cat([((phi[:, :1] - 1500.0) / 400.0).min(0).values.float(),
