@@ -241,6 +241,80 @@ def surrogate_bench(mech, ev, dev, n_train, epochs, n_eval, log=None):
                             "max_k |y_hat - y| / (|y| + 1e-3 rms_k)"}
 
 
+def lu_flops_per_state(nn):
+    """FP64 flops of one Newton-matrix factorisation: forming I - g J (one FMA
+    per entry), scaling the columns (one multiply per subdiagonal entry) and
+    the rank-1 updates (one FMA per trailing entry and pivot)."""
+    m = np.arange(1, nn)
+    return 2 * nn * nn + int(m.sum()) + 2 * int((m * m).sum())
+
+
+def implicit_bench(mech, ev, dev, n, order, steps, warmup, fp64_peak):
+    """Implicit-step consumer of the Jacobian on n device-resident states:
+    the Newton-matrix factorisation (pjg_lu_factor, dense Jacobian in, factors
+    to a separate array), one solve (pjg_lu_solve) and a whole ROS2 step
+    (pjg_ros2_step: 2 rates, 1 Jacobian, 1 factorisation, 2 solves).  Each
+    timed alone with CUDA events over `steps` repetitions after `warmup`."""
+    import torch
+    integ = pkg("integrate")
+    lib = pkg("_lib")
+    nn = mech.nn
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=2024, x_floor=1e-12)
+    tP = torch.from_numpy(P).to(dev)
+    tphi = torch.from_numpy(np.ascontiguousarray(phi.T) if order == "F" else phi).to(dev)
+    h = torch.from_numpy(10.0 ** np.random.default_rng(5).uniform(-9, -6, n)).to(dev)
+    jac = ev.jacobian(tP, tphi, order=order)
+    lu = torch.empty_like(jac)
+    b = torch.randn(tphi.shape, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        for _ in range(max(3, warmup)):
+            fn()
+        torch.cuda.synchronize()
+        l0 = lib.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, (lib.launch_count() - l0) / steps
+
+    piv = [None]
+
+    def factor():
+        piv[0] = integ.lu_factor(jac, h, s=integ.ROS2_GAMMA, order=order, out=lu)[1]
+
+    f_ms, f_launch = timed(factor)
+    s_ms, s_launch = timed(lambda: integ.lu_solve(lu, piv[0], b, order=order))
+    del jac, lu
+    torch.cuda.empty_cache()
+    st = integ.Ros2Stepper(ev, n, order=order)
+    y = torch.empty_like(tphi)
+    err = torch.empty_like(tphi)
+    r_ms, r_launch = timed(lambda: st.step(tP, tphi, h, out=y, err=err))
+    fl = lu_flops_per_state(nn)
+    f_rate = n / (f_ms * 1e-3)
+    lu_bytes = 8 * nn * nn
+    res = {"states": n, "order": order, "h": "per state, log-uniform 1e-9 .. 1e-6 s",
+           "factor": {"kernel": "lu_factor_kernel (one warp per state, matrix in shared memory)",
+                      "ms": f_ms, "states_per_s": f_rate, "launches": f_launch,
+                      "flops_per_state": fl, "fp64_tflops": fl * f_rate / 1e12,
+                      "fp64_frac": fl * f_rate / 1e12 / fp64_peak,
+                      "fp64_peak_source": "measured DFMA probe (pjg_fp64_peak)",
+                      "hbm_gbs": 2 * lu_bytes * f_rate / 1e9},
+           "solve": {"kernel": "lu_solve_kernel (one thread per state)", "ms": s_ms,
+                     "states_per_s": n / (s_ms * 1e-3), "launches": s_launch,
+                     "alg_bytes_per_state": lu_bytes + 4 * nn + 16 * nn,
+                     "hbm_gbs": (lu_bytes + 20 * nn) * n / (s_ms * 1e-3) / 1e9},
+           "ros2_step": {"ms": r_ms, "states_per_s": n / (r_ms * 1e-3), "launches": r_launch,
+                         "path": "Ros2Stepper.step -> pjg_ros2_step"}}
+    del st, y, err
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -278,6 +352,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-implicit", action="store_true",
+                    help="skip the implicit-step block (Newton-matrix LU, solve, ROS2 step)")
     ap.add_argument("--sur-train", type=int, default=1 << 22)
     ap.add_argument("--sur-epochs", type=int, default=12)
     ap.add_argument("--sur-eval", type=int, default=1 << 22)
@@ -429,6 +505,14 @@ def main():
     if rank == 0 and not args.no_cpu and args.kernel == "jacobian":
         cpu, _ = cpu_reference_run(mech, args.cpu_sample, 1, mech_name=args.mech)
 
+    implicit = None
+    if not args.no_implicit and args.kernel == "jacobian" and nn <= 169:
+        del out
+        torch.cuda.empty_cache()
+        out = None
+        implicit = implicit_bench(mech, ev, dev, n, args.order, args.steps, args.warmup,
+                                  fp64_peak.value)
+
     sur = None
     if not args.no_surrogate and args.kernel == "jacobian" and args.mech == "gri30":
         del out
@@ -454,7 +538,8 @@ def main():
                            "l2": "inputs %.0f MB and outputs %.0f MB, both larger than L2 (126 MB): "
                                  "no flush" % (8e-6 * n_in * n, 8e-6 * n_out * n)},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": launches, "clocks": clk, "surrogate": sur}
+                "gpu_launches": launches, "clocks": clk, "surrogate": sur,
+                "implicit_step": implicit}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -205,6 +205,39 @@ int pjg_read_initial_conditions(const char* filename, int64_t n, int32_t nn, cha
 int pjg_write_initial_conditions(const char* filename, int64_t n, int32_t nn, char order,
                                  const double* param, const double* phi);
 
+/* Linearly implicit integrator step on device arrays (asynchronous on
+ * `stream`).  No reference counterpart: the reference names coupling its
+ * Jacobians to Rosenbrock solvers as future work; these are that consumer.
+ *
+ * pjg_lu_factor: per state i, M_i = I - s h_i J_i (h_i = h[i], or h0 when h
+ * is NULL; s h_i rounded once, then each entry fma(-s h_i, J, delta)),
+ * factorised as P M = L U by LAPACK dgetf2's algorithm (partial pivoting on the
+ * first largest |a|, whole-row interchanges, column scaled by 1/pivot when
+ * |pivot| >= DBL_MIN, rank-1 update by FMA).  jac and lu are dense nn x nn
+ * per state in the layout pjg_jacobian writes (order 'C': [n][nn][nn]
+ * row-major; 'F': i + n*(row + nn*col)); lu may equal jac.  L (unit
+ * diagonal, not stored) below and U on and above the diagonal.  piv: nn
+ * 1-based row interchanges per state, laid out like phi; info[n] (optional):
+ * 0, or k for the first exactly zero pivot U(k,k) (1-based; LAPACK's info).
+ * 1 <= nn <= 169 (the matrix of one state lives in shared memory);
+ * larger mechanisms return PJG_ERR_UNSUPPORTED.
+ * pjg_lu_solve: b (laid out like phi) <- M^-1 b from pjg_lu_factor's output.
+ * pjg_ros2_step: one step of the L-stable Rosenbrock method ROS2
+ * (gamma = 1 + 1/sqrt 2) from phi with step h_i: rates and dense Jacobian at
+ * phi, one factorisation, two solves, one more rates evaluation;
+ * phi_new = phi + 1.5 h k1 + 0.5 h k2 and, if err is not NULL, the embedded
+ * first-order error estimate err = 0.5 h (k1 + k2).  Work arrays: jac_work
+ * n*nn*nn doubles (holds the factors on return), piv_work n*nn int32,
+ * vec_work 2*n*nn doubles (k1, k2 on return).  phi_new must not alias phi. */
+int pjg_lu_factor(int32_t nn, int64_t n, char order, double s, const double* h, double h0,
+                  const double* jac, double* lu, int32_t* piv, int32_t* info, void* stream);
+int pjg_lu_solve(int32_t nn, int64_t n, char order, const double* lu, const int32_t* piv,
+                 double* b, void* stream);
+int pjg_ros2_step(pjg_mech* mech, int64_t n, char order, int conp, const double* param,
+                  const double* phi, const double* h, double h0, double* phi_new, double* err,
+                  double* jac_work, int32_t* piv_work, double* vec_work, int32_t* info,
+                  void* stream);
+
 /* Copy the last error message of this thread into buf (always NUL-terminated). */
 int pjg_last_error(char* buf, size_t len);
 

@@ -203,6 +203,81 @@ class Oracle(object):
         return tuple(out)
 
 
+def _lu_lib():
+    lib = ctypes.CDLL(build())
+    lib.orc_lu_factor.restype = ctypes.c_int
+    lib.orc_lu_factor.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_double, _D, ctypes.c_double,
+                                  _D, _D, _I, _I]
+    lib.orc_lu_solve.restype = ctypes.c_int
+    lib.orc_lu_solve.argtypes = [ctypes.c_int, ctypes.c_long, _D, _I, _D]
+    lib.orc_ros2_combine.restype = ctypes.c_int
+    lib.orc_ros2_combine.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, _D, ctypes.c_double,
+                                     _D, _D, _D, _D, _D]
+    return lib
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(_D)
+
+
+def lu_factor(jac, s, h):
+    """M_i = I - s h_i J_i for jac (n, nn, nn) C order, h scalar or (n,):
+    LU with partial pivoting (orc_lu_factor) -> (lu (n, nn, nn), piv (n, nn)
+    1-based, info (n,))."""
+    jac = np.ascontiguousarray(jac, dtype=np.float64)
+    n, nn = jac.shape[0], jac.shape[1]
+    lu = np.empty_like(jac)
+    piv = np.empty((n, nn), dtype=np.int32)
+    info = np.empty(n, dtype=np.int32)
+    harr = None if np.ndim(h) == 0 else np.ascontiguousarray(h, dtype=np.float64)
+    rc = _lu_lib().orc_lu_factor(nn, n, float(s), _dp(harr), float(h) if harr is None else 0.0,
+                                 _dp(jac), _dp(lu), piv.ctypes.data_as(_I), info.ctypes.data_as(_I))
+    if rc != 0:
+        raise RuntimeError("oracle returned %d" % rc)
+    return lu, piv, info
+
+
+def lu_solve(lu, piv, b):
+    """b (n, nn) -> M^-1 b from lu_factor's factors (orc_lu_solve)."""
+    lu = np.ascontiguousarray(lu, dtype=np.float64)
+    piv = np.ascontiguousarray(piv, dtype=np.int32)
+    x = np.array(b, dtype=np.float64, order="C", copy=True)
+    rc = _lu_lib().orc_lu_solve(lu.shape[1], lu.shape[0], _dp(lu), piv.ctypes.data_as(_I), _dp(x))
+    if rc != 0:
+        raise RuntimeError("oracle returned %d" % rc)
+    return x
+
+
+def ros2_combine(op, h, x, k, z=None):
+    """ROS2 stage arithmetic (orc_ros2_combine), C order (n, nn) arrays."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    z = None if z is None else np.ascontiguousarray(z, dtype=np.float64)
+    n, nn = x.shape
+    out = np.empty_like(x)
+    err = np.empty_like(x) if op == 2 else None
+    harr = None if np.ndim(h) == 0 else np.ascontiguousarray(h, dtype=np.float64)
+    _lu_lib().orc_ros2_combine(op, nn, n, _dp(harr), float(h) if harr is None else 0.0, _dp(x),
+                               _dp(k), _dp(z), _dp(out), _dp(err))
+    return (out, err) if op == 2 else out
+
+
+ROS2_GAMMA = 1.7071067811865475  # 1 + 1/sqrt(2)
+
+
+def ros2_step(oracle, param, phi, h, conp=True):
+    """One ROS2 step (Verwer, Spee, Blom and Hundsdorfer 1999) with the
+    oracle's rates and Jacobian: returns (phi_new, err, info)."""
+    k1 = oracle.species_rates(param, phi, conp=conp)
+    lu, piv, info = lu_factor(oracle.jacobian(param, phi, conp=conp), ROS2_GAMMA, h)
+    k1 = lu_solve(lu, piv, k1)
+    y1 = ros2_combine(0, h, phi, k1)
+    k2 = ros2_combine(1, h, oracle.species_rates(param, y1, conp=conp), k1)
+    k2 = lu_solve(lu, piv, k2)
+    out, err = ros2_combine(2, h, phi, k1, k2)
+    return out, err, info
+
+
 class RefKernels(object):
     """The reference's shipped generated kernels, shim-compiled into oracle/_ref.
 

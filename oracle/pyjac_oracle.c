@@ -18,6 +18,7 @@
  */
 #include "pyjac_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -887,6 +888,110 @@ int orc_chem_utils(const orc_mech* m, long n, int conp, const double* phi, doubl
             h[i * ns + k] = conp ? RU * (hpoly + a[5]) : RU * (hpoly - Tc + a[5]);
             b[i * ns + k] = Tc * (Tc * (Tc * (Tc * a[4] / 20.0 + a[3] / 12.0) + a[2] / 6.0) + a[1] / 2.0) +
                             (a[0] + -1.0) * logT + -1.0 * a[0] + a[6] + -1.0 * a[5] * Tinv;
+        }
+    }
+    return 0;
+}
+
+/* ---- Newton-matrix LU of an implicit integrator step (no reference
+ * counterpart; the algorithm is LAPACK's unblocked dgetf2 and dgetrs, with the
+ * operation order of the CUDA kernels so that results agree bit for bit:
+ * entries fma(-s h_i, J, delta), pivot = first largest |a| in the column,
+ * whole-row interchange, scale by 1/pivot (or divide below DBL_MIN), rank-1
+ * update a_rc = fma(-l_r, u_c, a_rc); solves accumulate each row's dot product
+ * in increasing column order by FMA and divide by U's diagonal). */
+int orc_lu_factor(int nn, long n, double s, const double* h, double h0, const double* jac,
+                  double* lu, int* piv, int* info)
+{
+    if (nn < 1 || n < 0 || (n && (!jac || !lu || !piv))) return -1;
+    for (long i = 0; i < n; ++i) {
+        const double g = s * (h ? h[i] : h0);
+        const double* J = jac + (size_t)i * nn * nn;
+        double* a = lu + (size_t)i * nn * nn;
+        int first_zero = 0;
+        for (int r = 0; r < nn; ++r)
+            for (int c = 0; c < nn; ++c) a[r * nn + c] = fma(-g, J[r * nn + c], r == c ? 1.0 : 0.0);
+        for (int k = 0; k < nn; ++k) {
+            int br = k;
+            double best = fabs(a[k * nn + k]);
+            for (int r = k + 1; r < nn; ++r)
+                if (fabs(a[r * nn + k]) > best) {
+                    best = fabs(a[r * nn + k]);
+                    br = r;
+                }
+            piv[(size_t)i * nn + k] = br + 1;
+            const double p = a[br * nn + k];
+            if (p != 0.0) {
+                if (br != k)
+                    for (int c = 0; c < nn; ++c) {
+                        const double t = a[k * nn + c];
+                        a[k * nn + c] = a[br * nn + c];
+                        a[br * nn + c] = t;
+                    }
+                if (fabs(p) >= DBL_MIN) {
+                    const double inv = 1.0 / p;
+                    for (int r = k + 1; r < nn; ++r) a[r * nn + k] *= inv;
+                } else {
+                    for (int r = k + 1; r < nn; ++r) a[r * nn + k] /= p;
+                }
+            } else if (!first_zero) {
+                first_zero = k + 1;
+            }
+            for (int r = k + 1; r < nn; ++r)
+                for (int c = k + 1; c < nn; ++c)
+                    a[r * nn + c] = fma(-a[r * nn + k], a[k * nn + c], a[r * nn + c]);
+        }
+        if (info) info[i] = first_zero;
+    }
+    return 0;
+}
+
+int orc_lu_solve(int nn, long n, const double* lu, const int* piv, double* b)
+{
+    if (nn < 1 || n < 0 || (n && (!lu || !piv || !b))) return -1;
+    for (long i = 0; i < n; ++i) {
+        const double* a = lu + (size_t)i * nn * nn;
+        double* y = b + (size_t)i * nn;
+        for (int k = 0; k < nn; ++k) {
+            const int p = piv[(size_t)i * nn + k] - 1;
+            if (p != k) {
+                const double t = y[k];
+                y[k] = y[p];
+                y[p] = t;
+            }
+        }
+        for (int r = 1; r < nn; ++r) {
+            double acc = y[r];
+            for (int c = 0; c < r; ++c) acc = fma(-a[r * nn + c], y[c], acc);
+            y[r] = acc;
+        }
+        for (int r = nn - 1; r >= 0; --r) {
+            double acc = y[r];
+            for (int c = r + 1; c < nn; ++c) acc = fma(-a[r * nn + c], y[c], acc);
+            y[r] = acc / a[r * nn + r];
+        }
+    }
+    return 0;
+}
+
+/* ROS2 stage arithmetic, element-wise with a per-state step (C order):
+ * op 0: out = x + h k; op 1: out = x - 2 k; op 2: out = x + h (1.5 k + 0.5 z),
+ * err = h (0.5 (k + z)). */
+int orc_ros2_combine(int op, int nn, long n, const double* h, double h0, const double* x,
+                     const double* k, const double* z, double* out, double* err)
+{
+    for (long i = 0; i < n; ++i) {
+        const double hi = h ? h[i] : h0;
+        for (int j = 0; j < nn; ++j) {
+            const size_t e = (size_t)i * nn + j;
+            if (op == 0) {
+                out[e] = fma(hi, k[e], x[e]);
+            } else if (op == 1) {
+                out[e] = fma(-2.0, k[e], x[e]);
+            } else {
+                out[e] = fma(hi, fma(1.5, k[e], 0.5 * z[e]), x[e]);
+                if (err) err[e] = hi * (0.5 * (k[e] + z[e]));
+            }
         }
     }
     return 0;

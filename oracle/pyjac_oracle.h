@@ -86,6 +86,16 @@ int orc_rates_scale(const orc_mech* m, long n, int conp, const double* param,
  * out[i][k] for k < ns. */
 int orc_chem_utils(const orc_mech* m, long n, int conp, const double* phi, double* cp,
                    double* h, double* b);
+/* Newton matrix of an implicit step, M_i = I - s h_i J_i (h NULL: h0), LU with
+ * partial pivoting (LAPACK dgetf2's algorithm), C order only: jac, lu
+ * [n][nn][nn], piv [n][nn] 1-based, info [n] (may be NULL).  lu may equal jac. */
+int orc_lu_factor(int nn, long n, double s, const double* h, double h0, const double* jac,
+                  double* lu, int* piv, int* info);
+/* b [n][nn] <- M^-1 b from orc_lu_factor's factors */
+int orc_lu_solve(int nn, long n, const double* lu, const int* piv, double* b);
+/* stage arithmetic of the ROS2 Rosenbrock step, C order */
+int orc_ros2_combine(int op, int nn, long n, const double* h, double h0, const double* x,
+                     const double* k, const double* z, double* out, double* err);
 
 #ifdef __cplusplus
 }

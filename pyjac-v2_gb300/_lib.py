@@ -71,6 +71,14 @@ SIGNATURES = [
      [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_char, _VP, _VP]),
     ("pjg_chem_utils", ctypes.c_int,
      [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, _VP, _VP, _VP, _VP, _VP]),
+    ("pjg_lu_factor", ctypes.c_int,
+     [ctypes.c_int32, ctypes.c_int64, ctypes.c_char, ctypes.c_double, _VP, ctypes.c_double, _VP,
+      _VP, _VP, _VP, _VP]),
+    ("pjg_lu_solve", ctypes.c_int,
+     [ctypes.c_int32, ctypes.c_int64, ctypes.c_char, _VP, _VP, _VP, _VP]),
+    ("pjg_ros2_step", ctypes.c_int,
+     [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, _VP, _VP, _VP, ctypes.c_double, _VP, _VP,
+      _VP, _VP, _VP, _VP, _VP]),
 ]
 
 

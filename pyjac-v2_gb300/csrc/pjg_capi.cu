@@ -713,6 +713,48 @@ int pjg_vjp(pjg_mech* m, int64_t n, char order, int conp, const double* param, c
     return run_eval(m, PJG_KIND_VJP, n, order, conp, 0, param, phi, out, (cudaStream_t)stream, v);
 }
 
+int pjg_internal_lu_factor(int32_t nn, int64_t n, char order, double s, const double* h, double h0,
+                           const double* jac, double* lu, int32_t* piv, int32_t* info,
+                           cudaStream_t st);
+int pjg_internal_lu_solve(int32_t nn, int64_t n, char order, const double* lu, const int32_t* piv,
+                          double* b, cudaStream_t st);
+int pjg_internal_ros2_combine(int op, int32_t nn, int64_t n, char order, const double* h, double h0,
+                              const double* x, const double* k, const double* z, double* out,
+                              double* err, cudaStream_t st);
+
+// One step of ROS2 (Verwer, Spee, Blom and Hundsdorfer, SIAM J. Sci. Comput.
+// 20(4), 1999), gamma = 1 + 1/sqrt(2):
+//   (I - gamma h J) k1 = f(y),  (I - gamma h J) k2 = f(y + h k1) - 2 k1,
+//   y_new = y + 1.5 h k1 + 0.5 h k2,  err = y_new - (y + h k1) = 0.5 h (k1 + k2),
+// with J the analytical Jacobian at y and f the species rates.
+int pjg_ros2_step(pjg_mech* m, int64_t n, char order, int conp, const double* param,
+                  const double* phi, const double* h, double h0, double* phi_new, double* err,
+                  double* jac_work, int32_t* piv_work, double* vec_work, int32_t* info,
+                  void* stream)
+{
+    if (!m) return fail(PJG_ERR_ARG, "null mechanism");
+    if (n < 0) return fail(PJG_ERR_ARG, "negative problem size");
+    if (n == 0) return 0;
+    if (!phi || !param || !phi_new || !jac_work || !piv_work || !vec_work)
+        return fail(PJG_ERR_ARG, "null array");
+    if (phi_new == phi) return fail(PJG_ERR_ARG, "phi_new must not alias phi");
+    const cudaStream_t st = (cudaStream_t)stream;
+    const int nn = m->nn;
+    const double gamma = 1.7071067811865475;  // 1 + 1/sqrt(2)
+    double* k1 = vec_work;
+    double* k2 = vec_work + (size_t)n * nn;
+    int rc = run_eval(m, PJG_SPECIES_RATES, n, order, conp, 0, param, phi, k1, st);
+    if (!rc) rc = run_eval(m, PJG_JACOBIAN, n, order, conp, PJG_JAC_FULL, param, phi, jac_work, st);
+    if (!rc) rc = pjg_internal_lu_factor(nn, n, order, gamma, h, h0, jac_work, jac_work, piv_work, info, st);
+    if (!rc) rc = pjg_internal_lu_solve(nn, n, order, jac_work, piv_work, k1, st);
+    if (!rc) rc = pjg_internal_ros2_combine(0, nn, n, order, h, h0, phi, k1, nullptr, phi_new, nullptr, st);
+    if (!rc) rc = run_eval(m, PJG_SPECIES_RATES, n, order, conp, 0, param, phi_new, k2, st);
+    if (!rc) rc = pjg_internal_ros2_combine(1, nn, n, order, h, h0, k2, k1, nullptr, k2, nullptr, st);
+    if (!rc) rc = pjg_internal_lu_solve(nn, n, order, jac_work, piv_work, k2, st);
+    if (!rc) rc = pjg_internal_ros2_combine(2, nn, n, order, h, h0, phi, k1, k2, phi_new, err, st);
+    return rc;
+}
+
 int pjg_kernel_create(pjg_mech* m, int kind, size_t problem_size, size_t work_size, char order,
                       int conp, int jac_format, pjg_kernel** out)
 {

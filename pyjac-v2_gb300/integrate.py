@@ -1,0 +1,123 @@
+"""Linearly implicit integration on this library's Jacobians (device arrays).
+
+The consumer of the Jacobian in real use: an implicit ODE solver factors the
+Newton matrix M = I - s h J of every state and solves with it once per stage.
+No reference counterpart (the reference lists coupling to Rosenbrock solvers
+as future work).  Everything runs in the CUDA library (include/pyjac_gb300.h:
+pjg_lu_factor, pjg_lu_solve, pjg_ros2_step) on the current torch stream.
+
+Layouts are the dense Jacobian's: order 'C' — jac and lu (N, NN, NN)
+[state, row, col]; order 'F' — (NN, NN, N) [col, row, state].  Vectors and
+pivots are laid out like phi: (N, NN) for 'C', (NN, N) for 'F'.  Step sizes
+are a Python float (the same for every state) or a CUDA float64 tensor of N
+per-state values.
+"""
+import torch
+
+from . import _lib
+from .api import _order
+
+ROS2_GAMMA = 1.7071067811865475  # 1 + 1/sqrt(2)
+
+
+def _stream(t):
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def _h_args(h, n):
+    if isinstance(h, torch.Tensor):
+        if not (h.is_cuda and h.dtype == torch.float64 and h.is_contiguous() and h.numel() == n):
+            raise ValueError("h must be a contiguous CUDA float64 tensor of %d values" % n)
+        return h.data_ptr(), 0.0
+    return None, float(h)
+
+
+def _check_f64(*ts):
+    for t in ts:
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.float64
+                and t.is_contiguous()):
+            raise TypeError("expected contiguous CUDA float64 tensors")
+
+
+def _n_of(jac, order):
+    if jac.dim() != 3:
+        raise ValueError("jac must be a dense (N, NN, NN) or (NN, NN, N) tensor")
+    nn = jac.shape[1]
+    n = jac.shape[0] if order == "C" else jac.shape[2]
+    if (order == "C" and jac.shape[2] != nn) or (order == "F" and jac.shape[0] != nn):
+        raise ValueError("jac must be square per state")
+    return n, nn
+
+
+def lu_factor(jac, h, s=1.0, order="C", out=None, info=True):
+    """Factor M_i = I - s h_i J_i with partial pivoting (LAPACK dgetf2's
+    algorithm).  Returns (lu, piv, info): lu like jac (``out=jac`` factors in
+    place), piv int32 1-based row interchanges laid out like phi, info int32
+    (N,) = 0 or the 1-based index of the first exactly zero pivot."""
+    _check_f64(jac)
+    n, nn = _n_of(jac, order)
+    lu = torch.empty_like(jac) if out is None else out
+    _check_f64(lu)
+    if lu.shape != jac.shape:
+        raise ValueError("out must match jac")
+    piv = torch.empty((n, nn) if order == "C" else (nn, n), dtype=torch.int32, device=jac.device)
+    inf = torch.empty(n, dtype=torch.int32, device=jac.device) if info else None
+    hp, h0 = _h_args(h, n)
+    _lib.check("pjg_lu_factor", _lib.load().pjg_lu_factor(
+        nn, n, _order(order), float(s), hp, h0, jac.data_ptr(), lu.data_ptr(), piv.data_ptr(),
+        None if inf is None else inf.data_ptr(), _stream(jac)))
+    return lu, piv, inf
+
+
+def lu_solve(lu, piv, b, order="C"):
+    """b <- M^-1 b in place from lu_factor's output; returns b."""
+    _check_f64(lu, b)
+    n, nn = _n_of(lu, order)
+    if b.numel() != n * nn or piv.numel() != n * nn or piv.dtype != torch.int32:
+        raise ValueError("b and piv must hold N x NN values")
+    _lib.check("pjg_lu_solve", _lib.load().pjg_lu_solve(
+        nn, n, _order(order), lu.data_ptr(), piv.data_ptr(), b.data_ptr(), _stream(lu)))
+    return b
+
+
+class Ros2Stepper(object):
+    """Steps of the L-stable two-stage Rosenbrock method ROS2 (Verwer, Spee,
+    Blom and Hundsdorfer, SIAM J. Sci. Comput. 20(4), 1999) for up to
+    ``capacity`` states of one mechanism:
+
+        (I - gamma h J) k1 = f(y),  (I - gamma h J) k2 = f(y + h k1) - 2 k1,
+        y_new = y + 1.5 h k1 + 0.5 h k2,  err = 0.5 h (k1 + k2)
+
+    with f the species rates and J the analytical Jacobian at y
+    (gamma = 1 + 1/sqrt 2).  The work arrays (a dense Jacobian per state) are
+    allocated once; after a step ``lu`` and ``piv`` hold the factors of the
+    step's Newton matrix."""
+
+    def __init__(self, evaluator, capacity, order="C", device=None):
+        self.ev = evaluator
+        self.order = order
+        self.capacity = int(capacity)
+        nn = evaluator.nn
+        dev = device or torch.device("cuda", torch.cuda.current_device())
+        n = max(self.capacity, 1)
+        self.lu = torch.empty((n, nn, nn) if order == "C" else (nn, nn, n), dtype=torch.float64,
+                              device=dev)
+        self.piv = torch.empty((n, nn) if order == "C" else (nn, n), dtype=torch.int32, device=dev)
+        self.vec = torch.empty(2 * n * nn, dtype=torch.float64, device=dev)
+        self.info = torch.empty(n, dtype=torch.int32, device=dev)
+
+    def step(self, param, phi, h, conp=True, out=None, err=None):
+        """One step from phi; returns (phi_new, err, info)."""
+        n, st = self.ev._prep(param, phi, self.order)
+        if n != self.capacity:
+            raise ValueError("the stepper was sized for %d states" % self.capacity)
+        if out is None:
+            out = torch.empty_like(phi)
+        if err is None:
+            err = torch.empty_like(phi)
+        hp, h0 = _h_args(h, n)
+        _lib.check("pjg_ros2_step", self.ev._lib.pjg_ros2_step(
+            self.ev.handle, n, _order(self.order), int(bool(conp)), param.data_ptr(), phi.data_ptr(),
+            hp, h0, out.data_ptr(), err.data_ptr(), self.lu.data_ptr(), self.piv.data_ptr(),
+            self.vec.data_ptr(), self.info.data_ptr(), st))
+        return out, err, self.info[:n]
