@@ -298,7 +298,7 @@ def implicit_bench(mech, ev, dev, n, order, steps, warmup, fp64_peak):
     f_rate = n / (f_ms * 1e-3)
     lu_bytes = 8 * nn * nn
     res = {"states": n, "order": order, "h": "per state, log-uniform 1e-9 .. 1e-6 s",
-           "factor": {"kernel": "lu_factor_kernel (one warp per state, matrix in shared memory)",
+           "factor": {"kernel": "lu_factor_kernel (one block of 2 warps per state, matrix in shared memory)",
                       "ms": f_ms, "states_per_s": f_rate, "launches": f_launch,
                       "flops_per_state": fl, "fp64_tflops": fl * f_rate / 1e12,
                       "fp64_frac": fl * f_rate / 1e12 / fp64_peak,

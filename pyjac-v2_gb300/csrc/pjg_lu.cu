@@ -13,10 +13,10 @@
 // pivots as vectors of int32 (1-based, LAPACK's ipiv).
 //
 // FP64 on GB300 issues one warp instruction per 16 clocks per SM whatever the
-// number of active lanes, so the factorisation gives each state a whole warp
-// and spreads the flattened trailing block over the lanes (one state per
-// warp, its matrix in shared memory); the solve, which reads each factor
-// entry once, is one thread per state and bound by HBM.
+// number of active lanes, so the factorisation spreads each state's flattened
+// trailing block over the threads of a block (one state per block, its matrix
+// in shared memory) to keep the lanes full; the solve, which reads each
+// factor entry once, is one thread per state and bound by HBM.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -42,45 +42,82 @@ __device__ __forceinline__ size_t vec_idx(bool F, long long i, long long n, int 
     return F ? (size_t)(i + n * r) : (size_t)(i * (long long)nn + r);
 }
 
-// advance a flattened (row, column) cursor of an m-column block by 32 elements
-__device__ __forceinline__ void adv32(int& r, int& c, int m)
-{
-    c += 32;
-    while (c >= m) {
-        c -= m;
-        ++r;
+// Flattened (row, column) cursor over an m-column block, advanced by a fixed
+// stride T = q m + rem (q = T / m, rem = T % m): at most one wrap per step.
+struct Cursor {
+    int r, c, q, rem, m;
+    __device__ __forceinline__ Cursor(int start, int stride, int m_) : m(m_)
+    {
+        r = start / m;
+        c = start - r * m;
+        q = stride / m;
+        rem = stride - q * m;
     }
-}
+    __device__ __forceinline__ void next()
+    {
+        c += rem;
+        r += q;
+        if (c >= m) {
+            c -= m;
+            ++r;
+        }
+    }
+};
+
+constexpr long long kAbsMask = 0x7fffffffffffffffLL;
+constexpr long long kDblMinBits = 0x0010000000000000LL;  // bits of DBL_MIN
+
+// One state per block of LU_WARPS warps, its matrix in shared memory (odd
+// row pitch: a column read by 32 lanes is free of bank conflicts).  Step k:
+// every warp finds the pivot (integer comparison of |a| bit patterns, no
+// FP64 instruction); warp 0 forms the interchanged multiplier column scaled
+// by the reciprocal into lvec while all threads interchange the other
+// columns of rows k and p; after a barrier the trailing block gets the rank-1
+// update (elements spread flat over the block's threads, LU_BATCH per thread at
+// a time) and column k takes lvec; a second barrier closes the step.
+#ifndef LU_WARPS
+#define LU_WARPS 2  // 193 ms per 1M GRI states; 1, 3 and 4 warps: 201, 211, 205 ms
+#endif
+#ifndef LU_MINB
+#define LU_MINB 9
+#endif
+#ifndef LU_BATCH
+#define LU_BATCH 4  // trailing elements a thread loads before it stores
+#endif
+#define LU_THREADS (32 * LU_WARPS)
 
 template <bool F>
-__global__ void __launch_bounds__(256) lu_factor_kernel(int nn, long long n, double s,
-                                                        const double* __restrict__ h, double h0,
-                                                        const double* jac, double* lu,
-                                                        int32_t* __restrict__ piv,
-                                                        int32_t* __restrict__ info, int wpb)
+__global__ void __launch_bounds__(LU_THREADS, LU_MINB) lu_factor_kernel(int nn, long long n, double s,
+                                                                  const double* __restrict__ h,
+                                                                  double h0, const double* jac,
+                                                                  double* lu,
+                                                                  int32_t* __restrict__ piv,
+                                                                  int32_t* __restrict__ info)
 {
     extern __shared__ double smem[];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int pitch = nn | 1;  // odd pitch: a column read by 32 lanes is free of bank conflicts
-    double* a = smem + (size_t)w * nn * pitch;
-    int* sp = reinterpret_cast<int*>(smem + (size_t)wpb * nn * pitch) + w * nn;
-    const long long stride = (long long)gridDim.x * wpb;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int pitch = nn | 1;
+    double* a = smem;
+    double* lvec = a + (size_t)nn * pitch;
+    int* sp = reinterpret_cast<int*>(lvec + nn);
     const int nsq = nn * nn;
-    for (long long i = (long long)blockIdx.x * wpb + w; i < n; i += stride) {
+    for (long long i = blockIdx.x; i < n; i += gridDim.x) {
         const double g = s * (h ? h[i] : h0);
-        for (int e = lane; e < nsq; e += 32) {
-            const int r = e / nn, c = e - r * nn;
-            const double j = jac[mat_idx(F, i, n, nn, r, c)];
-            a[r * pitch + c] = fma(-g, j, r == c ? 1.0 : 0.0);
+        {
+            Cursor cu(tid, LU_THREADS, nn);
+            for (int e = tid; e < nsq; e += LU_THREADS) {
+                const double j = jac[mat_idx(F, i, n, nn, cu.r, cu.c)];
+                a[cu.r * pitch + cu.c] = fma(-g, j, cu.r == cu.c ? 1.0 : 0.0);
+                cu.next();
+            }
         }
-        __syncwarp();
-        int first_zero = 0;
+        __syncthreads();
+        int first_zero = 0;  // thread 0's
         for (int k = 0; k < nn; ++k) {
-            // pivot: first row of largest |a_rk|, r >= k (|x| compared as bit patterns)
             long long best = -1;
             int br = k;
             for (int r = k + lane; r < nn; r += 32) {
-                const long long v = __double_as_longlong(a[r * pitch + k]) & 0x7fffffffffffffffLL;
+                const long long v = __double_as_longlong(a[r * pitch + k]) & kAbsMask;
                 if (v > best) {
                     best = v;
                     br = r;
@@ -95,63 +132,71 @@ __global__ void __launch_bounds__(256) lu_factor_kernel(int nn, long long n, dou
                     br = orr;
                 }
             }
-            if (lane == 0) sp[k] = br + 1;
-            const double p = a[br * pitch + k];
+            const bool nonzero = best != 0;
             const int m = nn - k - 1;
-            if (p != 0.0) {
-                if (br != k)
-                    for (int c = lane; c < nn; c += 32) {
+            double p = 0.0;
+            if (warp == 0) {
+                p = a[br * pitch + k];
+                if (lane == 0) {
+                    sp[k] = br + 1;
+                    if (!nonzero && !first_zero) first_zero = k + 1;
+                }
+                const bool recip = best >= kDblMinBits;
+                const double inv = (nonzero && recip) ? __drcp_rn(p) : 0.0;
+                for (int r = k + 1 + lane; r < nn; r += 32) {
+                    double v = a[(r == br ? k : r) * pitch + k];
+                    if (nonzero) v = recip ? v * inv : v / p;
+                    lvec[r] = v;
+                }
+            }
+            if (nonzero && br != k)
+                for (int c = tid; c < nn; c += LU_THREADS)
+                    if (c != k) {
                         const double t = a[k * pitch + c];
                         a[k * pitch + c] = a[br * pitch + c];
                         a[br * pitch + c] = t;
                     }
-                __syncwarp();
-                if (fabs(p) >= DBL_MIN) {
-                    const double inv = 1.0 / p;
-                    for (int r = k + 1 + lane; r < nn; r += 32) a[r * pitch + k] *= inv;
-                } else {
-                    for (int r = k + 1 + lane; r < nn; r += 32) a[r * pitch + k] /= p;
-                }
-            } else if (!first_zero) {
-                first_zero = k + 1;
-            }
-            __syncwarp();
-            // rank-1 update of the m x m trailing block, four elements per lane at a time
+            __syncthreads();
+            if (tid == 0 && nonzero) a[k * pitch + k] = p;
+            for (int r = k + 1 + tid; r < nn; r += LU_THREADS) a[r * pitch + k] = lvec[r];
             const int mm = m * m;
-            if (mm > 0) {
+            if (tid < mm) {
                 const double* urow = a + k * pitch + k + 1;
-                const double* lcol = a + (k + 1) * pitch + k;
+                const double* lv = lvec + k + 1;
                 double* t = a + (k + 1) * pitch + k + 1;
-                int r = lane / m, c = lane - (lane / m) * m;
-                for (int e = lane; e < mm; e += 128) {
-                    int o[4];
-                    double l[4], u[4], v[4];
-                    bool ok[4];
+                Cursor cu(tid, LU_THREADS, m);
+                for (int e = tid; e < mm; e += LU_BATCH * LU_THREADS) {
+                    int o[LU_BATCH];
+                    double l[LU_BATCH], u[LU_BATCH], v[LU_BATCH];
+                    bool ok[LU_BATCH];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        ok[q] = e + 32 * q < mm;
-                        o[q] = r * pitch + c;
+                    for (int q = 0; q < LU_BATCH; ++q) {
+                        ok[q] = e + q * LU_THREADS < mm;
+                        o[q] = cu.r * pitch + cu.c;
                         if (ok[q]) {
-                            l[q] = lcol[r * pitch];
-                            u[q] = urow[c];
+                            l[q] = lv[cu.r];
+                            u[q] = urow[cu.c];
                             v[q] = t[o[q]];
                         }
-                        adv32(r, c, m);
+                        cu.next();
                     }
 #pragma unroll
-                    for (int q = 0; q < 4; ++q)
+                    for (int q = 0; q < LU_BATCH; ++q)
                         if (ok[q]) t[o[q]] = fma(-l[q], u[q], v[q]);
                 }
             }
-            __syncwarp();
+            __syncthreads();
         }
-        for (int e = lane; e < nsq; e += 32) {
-            const int r = e / nn, c = e - r * nn;
-            lu[mat_idx(F, i, n, nn, r, c)] = a[r * pitch + c];
+        {
+            Cursor cu(tid, LU_THREADS, nn);
+            for (int e = tid; e < nsq; e += LU_THREADS) {
+                lu[mat_idx(F, i, n, nn, cu.r, cu.c)] = a[cu.r * pitch + cu.c];
+                cu.next();
+            }
         }
-        for (int k = lane; k < nn; k += 32) piv[vec_idx(F, i, n, nn, k)] = sp[k];
-        if (lane == 0 && info) info[i] = first_zero;
-        __syncwarp();
+        for (int k = tid; k < nn; k += LU_THREADS) piv[vec_idx(F, i, n, nn, k)] = sp[k];
+        if (tid == 0 && info) info[i] = first_zero;
+        __syncthreads();
     }
 }
 
@@ -216,7 +261,7 @@ __global__ void ros2_combine_kernel(int op, int nn, long long n, const double* _
     }
 }
 
-int lu_factor_config(int nn, int* wpb, size_t* smem, int* grid)
+int lu_factor_config(int nn, size_t* smem, int* grid)
 {
     static int sms = 0;
     if (!sms) {
@@ -225,17 +270,14 @@ int lu_factor_config(int nn, int* wpb, size_t* smem, int* grid)
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
             return pjg_internal_fail(PJG_ERR_CUDA, "device query failed");
     }
-    const size_t per_warp = (size_t)nn * (nn | 1) * sizeof(double) + (size_t)nn * sizeof(int);
-    int w = (int)((48u << 10) / per_warp);
-    *wpb = w < 1 ? 1 : (w > 8 ? 8 : w);
-    *smem = per_warp * *wpb;
+    *smem = (size_t)nn * (nn | 1) * sizeof(double) + (size_t)nn * (sizeof(double) + sizeof(int));
     const void* fn = (const void*)lu_factor_kernel<false>;
     const void* fnF = (const void*)lu_factor_kernel<true>;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess ||
         cudaFuncSetAttribute(fnF, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess)
         return pjg_internal_fail(PJG_ERR_CUDA, "cannot reserve shared memory for the LU kernel");
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * *wpb, *smem) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, LU_THREADS, *smem) != cudaSuccess ||
         per_sm < 1)
         return pjg_internal_fail(PJG_ERR_CUDA, "LU kernel does not fit on the device");
     *grid = sms * per_sm;
@@ -253,15 +295,14 @@ extern "C" int pjg_internal_lu_factor(int32_t nn, int64_t n, char order, double 
     if (order != 'C' && order != 'F') return pjg_internal_fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
     if (n == 0) return 0;
     if (!jac || !lu || !piv) return pjg_internal_fail(PJG_ERR_ARG, "null array");
-    int wpb = 1, grid = 1;
+    int grid = 1;
     size_t smem = 0;
-    if (int rc = lu_factor_config(nn, &wpb, &smem, &grid)) return rc;
-    const long long need = (n + wpb - 1) / wpb;
-    if (need < grid) grid = (int)need;
+    if (int rc = lu_factor_config(nn, &smem, &grid)) return rc;
+    if (n < grid) grid = (int)n;
     if (order == 'F')
-        lu_factor_kernel<true><<<grid, 32 * wpb, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info, wpb);
+        lu_factor_kernel<true><<<grid, LU_THREADS, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
     else
-        lu_factor_kernel<false><<<grid, 32 * wpb, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info, wpb);
+        lu_factor_kernel<false><<<grid, LU_THREADS, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
     pjg_internal_count_launch();
     if (cudaGetLastError() != cudaSuccess) return pjg_internal_fail(PJG_ERR_CUDA, "LU factor launch failed");
     return 0;
