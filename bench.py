@@ -288,14 +288,25 @@ def implicit_bench(mech, ev, dev, n, order, steps, warmup, fp64_peak):
 
     f_ms, f_launch = timed(factor)
     s_ms, s_launch = timed(lambda: integ.lu_solve(lu, piv[0], b, order=order))
+    fs_ms, _ = timed(lambda: integ.lu_factor_sparse(ev, jac, h, s=integ.ROS2_GAMMA, order=order,
+                                                    out=lu))
+    ss_ms, _ = timed(lambda: integ.lu_solve_sparse(ev, lu, b, order=order))
     del jac, lu
     torch.cuda.empty_cache()
-    st = integ.Ros2Stepper(ev, n, order=order)
     y = torch.empty_like(tphi)
     err = torch.empty_like(tphi)
+    st = integ.Ros2Stepper(ev, n, order=order)
     r_ms, r_launch = timed(lambda: st.step(tP, tphi, h, out=y, err=err))
+    del st
+    torch.cuda.empty_cache()
+    st = integ.Ros2Stepper(ev, n, order=order, lu_kind="sparse")
+    rs_ms, _ = timed(lambda: st.step(tP, tphi, h, out=y, err=err))
     fl = lu_flops_per_state(nn)
     f_rate = n / (f_ms * 1e-3)
+    _, nnz_lu, fma_sp = integ.lu_plan_info(ev)
+    # forming the entries and the updates; the column scalings (about 2 % more) are not counted
+    fl_sp = 2 * nn * nn + 2 * fma_sp
+    fs_rate = n / (fs_ms * 1e-3)
     lu_bytes = 8 * nn * nn
     res = {"states": n, "order": order, "h": "per state, log-uniform 1e-9 .. 1e-6 s",
            "factor": {"kernel": "lu_factor_kernel (one block of 2 warps per state, matrix in shared memory)",
@@ -308,8 +319,18 @@ def implicit_bench(mech, ev, dev, n, order, steps, warmup, fp64_peak):
                      "states_per_s": n / (s_ms * 1e-3), "launches": s_launch,
                      "alg_bytes_per_state": lu_bytes + 4 * nn + 16 * nn,
                      "hbm_gbs": (lu_bytes + 20 * nn) * n / (s_ms * 1e-3) / 1e9},
+           "factor_sparse": {"kernel": "lu_sparse_kernel (static Markowitz order, no "
+                                       "interchanges, filled pattern only)",
+                             "ms": fs_ms, "states_per_s": fs_rate, "fma_per_state": fma_sp,
+                             "nnz_lu": nnz_lu, "flops_per_state": fl_sp,
+                             "fp64_tflops": fl_sp * fs_rate / 1e12,
+                             "fp64_frac": fl_sp * fs_rate / 1e12 / fp64_peak},
+           "solve_sparse": {"kernel": "lu_sparse_solve_kernel", "ms": ss_ms,
+                            "states_per_s": n / (ss_ms * 1e-3)},
            "ros2_step": {"ms": r_ms, "states_per_s": n / (r_ms * 1e-3), "launches": r_launch,
-                         "path": "Ros2Stepper.step -> pjg_ros2_step"}}
+                         "path": "Ros2Stepper.step -> pjg_ros2_step (partial pivoting)"},
+           "ros2_step_sparse": {"ms": rs_ms, "states_per_s": n / (rs_ms * 1e-3),
+                                "path": "Ros2Stepper(lu_kind='sparse').step -> pjg_ros2_step"}}
     del st, y, err
     torch.cuda.empty_cache()
     return res

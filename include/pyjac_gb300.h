@@ -222,21 +222,46 @@ int pjg_write_initial_conditions(const char* filename, int64_t n, int32_t nn, ch
  * 1 <= nn <= 169 (the matrix of one state lives in shared memory);
  * larger mechanisms return PJG_ERR_UNSUPPORTED.
  * pjg_lu_solve: b (laid out like phi) <- M^-1 b from pjg_lu_factor's output.
+ *
+ * Static-pivot sparse LU (the factorisation of implicit chemistry solvers
+ * such as KPP: no row interchanges).  The mechanism's Jacobian pattern plus
+ * the diagonal is ordered once by the Markowitz rule (the remaining diagonal
+ * entry with the least (row count - 1)(column count - 1), lowest index on
+ * ties; symmetric permutation perm[position] = variable) and factored
+ * symbolically; step k then updates only the filled pattern's rows x
+ * columns.  pjg_lu_symbolic: that order and the counts (FMAs per state,
+ * entries of L + U) for a CRS pattern, host only.  pjg_lu_plan_info: the same
+ * for a mechanism (the plan is built on first use and kept with it).
+ * pjg_lu_factor_sparse: M_i = I - s h_i J_i as for pjg_lu_factor, factored
+ * without interchanges in the permuted order: lu[i][r][c] (dense layout of
+ * jac) holds the factors of M_i[perm[r]][perm[c]] (zeros outside the filled
+ * pattern); info[i] = k for the first exactly zero pivot (1-based step).
+ * pjg_lu_solve_sparse: b (laid out like phi, variables' order) <- M^-1 b.
+ *
  * pjg_ros2_step: one step of the L-stable Rosenbrock method ROS2
  * (gamma = 1 + 1/sqrt 2) from phi with step h_i: rates and dense Jacobian at
- * phi, one factorisation, two solves, one more rates evaluation;
+ * phi, one factorisation (lu_kind 0: partial pivoting; 1: the static-pivot
+ * sparse plan), two solves, one more rates evaluation;
  * phi_new = phi + 1.5 h k1 + 0.5 h k2 and, if err is not NULL, the embedded
  * first-order error estimate err = 0.5 h (k1 + k2).  Work arrays: jac_work
- * n*nn*nn doubles (holds the factors on return), piv_work n*nn int32,
- * vec_work 2*n*nn doubles (k1, k2 on return).  phi_new must not alias phi. */
+ * n*nn*nn doubles (holds the factors on return), piv_work n*nn int32
+ * (lu_kind 0 only), vec_work 2*n*nn doubles (k1, k2 on return).  phi_new
+ * must not alias phi. */
 int pjg_lu_factor(int32_t nn, int64_t n, char order, double s, const double* h, double h0,
                   const double* jac, double* lu, int32_t* piv, int32_t* info, void* stream);
 int pjg_lu_solve(int32_t nn, int64_t n, char order, const double* lu, const int32_t* piv,
                  double* b, void* stream);
+int pjg_lu_symbolic(int32_t nn, const int32_t* row_ptr, const int32_t* col_ind, int32_t* perm,
+                    int32_t* nnz_lu, int64_t* fma_per_state);
+int pjg_lu_plan_info(pjg_mech* mech, int32_t* perm, int32_t* nnz_lu, int64_t* fma_per_state);
+int pjg_lu_factor_sparse(pjg_mech* mech, int64_t n, char order, double s, const double* h,
+                         double h0, const double* jac, double* lu, int32_t* info, void* stream);
+int pjg_lu_solve_sparse(pjg_mech* mech, int64_t n, char order, const double* lu, double* b,
+                        void* stream);
 int pjg_ros2_step(pjg_mech* mech, int64_t n, char order, int conp, const double* param,
-                  const double* phi, const double* h, double h0, double* phi_new, double* err,
-                  double* jac_work, int32_t* piv_work, double* vec_work, int32_t* info,
-                  void* stream);
+                  const double* phi, const double* h, double h0, int lu_kind, double* phi_new,
+                  double* err, double* jac_work, int32_t* piv_work, double* vec_work,
+                  int32_t* info, void* stream);
 
 /* Copy the last error message of this thread into buf (always NUL-terminated). */
 int pjg_last_error(char* buf, size_t len);

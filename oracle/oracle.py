@@ -210,6 +210,11 @@ def _lu_lib():
                                   _D, _D, _I, _I]
     lib.orc_lu_solve.restype = ctypes.c_int
     lib.orc_lu_solve.argtypes = [ctypes.c_int, ctypes.c_long, _D, _I, _D]
+    lib.orc_lu_sparse_factor.restype = ctypes.c_int
+    lib.orc_lu_sparse_factor.argtypes = [ctypes.c_int, ctypes.c_long, ctypes.c_double, _D,
+                                         ctypes.c_double, _D, _I, _I, _I, _I, _I, _D, _I]
+    lib.orc_lu_sparse_solve.restype = ctypes.c_int
+    lib.orc_lu_sparse_solve.argtypes = [ctypes.c_int, ctypes.c_long, _D, _I, _I, _I, _I, _I, _D]
     lib.orc_ros2_combine.restype = ctypes.c_int
     lib.orc_ros2_combine.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, _D, ctypes.c_double,
                                      _D, _D, _D, _D, _D]
@@ -262,18 +267,112 @@ def ros2_combine(op, h, x, k, z=None):
     return (out, err) if op == 2 else out
 
 
+def lu_plan(row_ptr, col_ind):
+    """Static-pivot plan of M = I - s h J for a CRS pattern (plus the
+    diagonal): the Markowitz order (at each step the remaining diagonal entry
+    with the least (row count - 1) x (column count - 1) over the remaining
+    submatrix, lowest index on ties; the pattern fills in as each step
+    eliminates), then the symbolic factorisation of the permuted pattern.
+    Returns a dict of int32 arrays: perm, roff/ridx (rows below each pivot),
+    coff/cidx (columns right of it), loff/lidx and uoff/uidx (the filled L and
+    U rows), plus nnz_lu and fma (FMAs per state)."""
+    rp = np.asarray(row_ptr)
+    ci = np.asarray(col_ind)
+    nn = rp.size - 1
+    A = np.eye(nn, dtype=bool)
+    for r in range(nn):
+        A[r, ci[rp[r]:rp[r + 1]]] = True
+    done = np.zeros(nn, dtype=bool)
+    perm = []
+    W = A.copy()
+    for _ in range(nn):
+        rem = ~done
+        best, bscore = -1, None
+        for v in np.nonzero(rem)[0]:
+            rc = int(W[v, rem].sum()) - 1
+            cc = int(W[rem, v].sum()) - 1
+            if bscore is None or rc * cc < bscore:
+                best, bscore = v, rc * cc
+        rows = [r for r in np.nonzero(rem & W[:, best])[0] if r != best]
+        cols = [c for c in np.nonzero(rem & W[best, :])[0] if c != best]
+        for r in rows:
+            W[r, cols] = True
+        done[best] = True
+        perm.append(int(best))
+    perm = np.array(perm, dtype=np.int32)
+    B = A[np.ix_(perm, perm)].copy()
+    roff, coff, ridx, cidx, fma = [0], [0], [], [], 0
+    for k in range(nn):
+        R = [r for r in range(k + 1, nn) if B[r, k]]
+        C = [c for c in range(k + 1, nn) if B[k, c]]
+        for r in R:
+            B[r, C] = True
+        fma += len(R) * len(C)
+        ridx += R
+        cidx += C
+        roff.append(len(ridx))
+        coff.append(len(cidx))
+    loff, uoff, lidx, uidx = [0], [0], [], []
+    for r in range(nn):
+        cols = np.nonzero(B[r])[0]
+        lidx += [int(c) for c in cols if c < r]
+        uidx += [int(c) for c in cols if c > r]
+        loff.append(len(lidx))
+        uoff.append(len(uidx))
+    a32 = lambda x: np.ascontiguousarray(np.array(x if len(x) else [0], dtype=np.int32))
+    return {"perm": perm, "roff": a32(roff), "ridx": a32(ridx), "coff": a32(coff),
+            "cidx": a32(cidx), "loff": a32(loff), "lidx": a32(lidx), "uoff": a32(uoff),
+            "uidx": a32(uidx), "nnz_lu": int(B.sum()), "fma": fma}
+
+
+def lu_factor_sparse(jac, s, h, plan):
+    """Static-pivot factorisation (orc_lu_sparse_factor) of M_i = I - s h_i J_i,
+    jac (n, nn, nn) C order -> (lu of the permuted matrix, info)."""
+    jac = np.ascontiguousarray(jac, dtype=np.float64)
+    n, nn = jac.shape[0], jac.shape[1]
+    lu = np.empty_like(jac)
+    info = np.empty(n, dtype=np.int32)
+    harr = None if np.ndim(h) == 0 else np.ascontiguousarray(h, dtype=np.float64)
+    ip = lambda k: plan[k].ctypes.data_as(_I)
+    rc = _lu_lib().orc_lu_sparse_factor(nn, n, float(s), _dp(harr), float(h) if harr is None else 0.0,
+                                        _dp(jac), ip("perm"), ip("roff"), ip("ridx"), ip("coff"),
+                                        ip("cidx"), _dp(lu), info.ctypes.data_as(_I))
+    if rc != 0:
+        raise RuntimeError("oracle returned %d" % rc)
+    return lu, info
+
+
+def lu_solve_sparse(lu, b, plan):
+    """b (n, nn) -> M^-1 b from lu_factor_sparse's factors (orc_lu_sparse_solve)."""
+    lu = np.ascontiguousarray(lu, dtype=np.float64)
+    x = np.array(b, dtype=np.float64, order="C", copy=True)
+    ip = lambda k: plan[k].ctypes.data_as(_I)
+    rc = _lu_lib().orc_lu_sparse_solve(lu.shape[1], lu.shape[0], _dp(lu), ip("perm"), ip("loff"),
+                                       ip("lidx"), ip("uoff"), ip("uidx"), _dp(x))
+    if rc != 0:
+        raise RuntimeError("oracle returned %d" % rc)
+    return x
+
+
 ROS2_GAMMA = 1.7071067811865475  # 1 + 1/sqrt(2)
 
 
-def ros2_step(oracle, param, phi, h, conp=True):
+def ros2_step(oracle, param, phi, h, conp=True, plan=None):
     """One ROS2 step (Verwer, Spee, Blom and Hundsdorfer 1999) with the
-    oracle's rates and Jacobian: returns (phi_new, err, info)."""
+    oracle's rates and Jacobian: returns (phi_new, err, info).  With a plan
+    (lu_plan) the Newton matrix is factored by the static-pivot sparse LU,
+    else with partial pivoting."""
     k1 = oracle.species_rates(param, phi, conp=conp)
-    lu, piv, info = lu_factor(oracle.jacobian(param, phi, conp=conp), ROS2_GAMMA, h)
-    k1 = lu_solve(lu, piv, k1)
+    J = oracle.jacobian(param, phi, conp=conp)
+    if plan is None:
+        lu, piv, info = lu_factor(J, ROS2_GAMMA, h)
+        solve = lambda b: lu_solve(lu, piv, b)
+    else:
+        lu, info = lu_factor_sparse(J, ROS2_GAMMA, h, plan)
+        solve = lambda b: lu_solve_sparse(lu, b, plan)
+    k1 = solve(k1)
     y1 = ros2_combine(0, h, phi, k1)
-    k2 = ros2_combine(1, h, oracle.species_rates(param, y1, conp=conp), k1)
-    k2 = lu_solve(lu, piv, k2)
+    k2 = solve(ros2_combine(1, h, oracle.species_rates(param, y1, conp=conp), k1))
     out, err = ros2_combine(2, h, phi, k1, k2)
     return out, err, info
 

@@ -996,3 +996,71 @@ int orc_ros2_combine(int op, int nn, long n, const double* h, double h0, const d
     }
     return 0;
 }
+
+/* ---- static-pivot sparse LU (no interchanges) on a precomputed plan: the
+ * permuted matrix a[r][c] = fma(-s h_i, J[perm[r]][perm[c]], delta) is
+ * eliminated in order; step k scales the rows R_k of column k by 1/pivot (or
+ * divides below DBL_MIN) and updates R_k x C_k by FMA.  Dense C-order
+ * storage of the permuted factors. */
+int orc_lu_sparse_factor(int nn, long n, double s, const double* h, double h0, const double* jac,
+                         const int* perm, const int* roff, const int* ridx, const int* coff,
+                         const int* cidx, double* lu, int* info)
+{
+    if (nn < 1 || n < 0) return -1;
+    for (long i = 0; i < n; ++i) {
+        const double g = s * (h ? h[i] : h0);
+        const double* J = jac + (size_t)i * nn * nn;
+        double* a = lu + (size_t)i * nn * nn;
+        int first_zero = 0;
+        for (int r = 0; r < nn; ++r)
+            for (int c = 0; c < nn; ++c)
+                a[r * nn + c] = fma(-g, J[perm[r] * nn + perm[c]], r == c ? 1.0 : 0.0);
+        for (int k = 0; k < nn; ++k) {
+            const double p = a[k * nn + k];
+            if (p == 0.0 && !first_zero) first_zero = k + 1;
+            if (roff[k + 1] == roff[k]) continue;
+            if (p != 0.0)
+                for (int q = roff[k]; q < roff[k + 1]; ++q) {
+                    const int r = ridx[q];
+                    if (fabs(p) >= DBL_MIN)
+                        a[r * nn + k] *= 1.0 / p;
+                    else
+                        a[r * nn + k] /= p;
+                }
+            for (int q = roff[k]; q < roff[k + 1]; ++q)
+                for (int t = coff[k]; t < coff[k + 1]; ++t) {
+                    const int r = ridx[q], c = cidx[t];
+                    a[r * nn + c] = fma(-a[r * nn + k], a[k * nn + c], a[r * nn + c]);
+                }
+        }
+        if (info) info[i] = first_zero;
+    }
+    return 0;
+}
+
+/* b [n][nn] (variables' order) <- M^-1 b from orc_lu_sparse_factor's factors */
+int orc_lu_sparse_solve(int nn, long n, const double* lu, const int* perm, const int* loff,
+                        const int* lidx, const int* uoff, const int* uidx, double* b)
+{
+    if (nn < 1 || n < 0) return -1;
+    double* y = (double*)malloc(sizeof(double) * (size_t)nn);
+    if (!y) return -2;
+    for (long i = 0; i < n; ++i) {
+        const double* a = lu + (size_t)i * nn * nn;
+        double* x = b + (size_t)i * nn;
+        for (int r = 0; r < nn; ++r) y[r] = x[perm[r]];
+        for (int r = 1; r < nn; ++r) {
+            double acc = y[r];
+            for (int q = loff[r]; q < loff[r + 1]; ++q) acc = fma(-a[r * nn + lidx[q]], y[lidx[q]], acc);
+            y[r] = acc;
+        }
+        for (int r = nn - 1; r >= 0; --r) {
+            double acc = y[r];
+            for (int q = uoff[r]; q < uoff[r + 1]; ++q) acc = fma(-a[r * nn + uidx[q]], y[uidx[q]], acc);
+            y[r] = acc / a[r * nn + r];
+        }
+        for (int r = 0; r < nn; ++r) x[perm[r]] = y[r];
+    }
+    free(y);
+    return 0;
+}

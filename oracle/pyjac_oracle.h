@@ -93,6 +93,13 @@ int orc_lu_factor(int nn, long n, double s, const double* h, double h0, const do
                   double* lu, int* piv, int* info);
 /* b [n][nn] <- M^-1 b from orc_lu_factor's factors */
 int orc_lu_solve(int nn, long n, const double* lu, const int* piv, double* b);
+/* static-pivot sparse LU on a plan (permutation, per-step row and column
+ * lists R_k, C_k, and the filled pattern's L and U rows), C order */
+int orc_lu_sparse_factor(int nn, long n, double s, const double* h, double h0, const double* jac,
+                         const int* perm, const int* roff, const int* ridx, const int* coff,
+                         const int* cidx, double* lu, int* info);
+int orc_lu_sparse_solve(int nn, long n, const double* lu, const int* perm, const int* loff,
+                        const int* lidx, const int* uoff, const int* uidx, double* b);
 /* stage arithmetic of the ROS2 Rosenbrock step, C order */
 int orc_ros2_combine(int op, int nn, long n, const double* h, double h0, const double* x,
                      const double* k, const double* z, double* out, double* err);

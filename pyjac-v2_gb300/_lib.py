@@ -77,8 +77,15 @@ SIGNATURES = [
     ("pjg_lu_solve", ctypes.c_int,
      [ctypes.c_int32, ctypes.c_int64, ctypes.c_char, _VP, _VP, _VP, _VP]),
     ("pjg_ros2_step", ctypes.c_int,
-     [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, _VP, _VP, _VP, ctypes.c_double, _VP, _VP,
-      _VP, _VP, _VP, _VP, _VP]),
+     [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, _VP, _VP, _VP, ctypes.c_double, ctypes.c_int,
+      _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    ("pjg_lu_symbolic", ctypes.c_int,
+     [ctypes.c_int32, _VP, _VP, _VP, _VP, ctypes.POINTER(ctypes.c_int64)]),
+    ("pjg_lu_plan_info", ctypes.c_int, [_VP, _VP, _VP, ctypes.POINTER(ctypes.c_int64)]),
+    ("pjg_lu_factor_sparse", ctypes.c_int,
+     [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_double, _VP, ctypes.c_double, _VP, _VP, _VP,
+      _VP]),
+    ("pjg_lu_solve_sparse", ctypes.c_int, [_VP, ctypes.c_int64, ctypes.c_char, _VP, _VP, _VP]),
 ]
 
 

@@ -71,6 +71,16 @@ struct SlotTables {
 
 }  // namespace
 
+extern "C" int pjg_internal_lu_plan_create(int32_t nn, const int32_t* row_ptr, const int32_t* col_ind,
+                                           void** out);
+extern "C" void pjg_internal_lu_plan_destroy(void* p);
+extern "C" void pjg_internal_lu_plan_info(const void* p, int32_t* perm, int32_t* nnz_lu, int64_t* fma);
+extern "C" int pjg_internal_lu_factor_sparse(const void* p, int64_t n, char order, double s,
+                                             const double* h, double h0, const double* jac, double* lu,
+                                             int32_t* info, cudaStream_t st);
+extern "C" int pjg_internal_lu_solve_sparse(const void* p, int64_t n, char order, const double* lu,
+                                            double* b, cudaStream_t st);
+
 struct pjg_mech {
     int ns = 0, nr = 0, nn = 0, need_logP = 0, nnz = 0, jac_approx = 0;
     int device = 0;
@@ -88,6 +98,8 @@ struct pjg_mech {
     // working buffer shared by device-pointer calls on this mechanism
     double* work = nullptr;
     size_t work_bytes = 0;
+    // static-pivot sparse LU plan of the Newton matrix (built on first use)
+    void* lu_plan = nullptr;
 };
 
 // Kernel object (host-pointer calls).  A call streams the problem through
@@ -658,6 +670,7 @@ int pjg_mech_destroy(pjg_mech* m)
     cudaFree(m->thd_coef);
     cudaFree(m->aux);
     cudaFree(m->work);
+    pjg_internal_lu_plan_destroy(m->lu_plan);
     for (auto& kv : m->slots) {
         SlotTables& t = kv.second;
         cudaFree(t.rxn_slot_off);
@@ -722,35 +735,87 @@ int pjg_internal_ros2_combine(int op, int32_t nn, int64_t n, char order, const d
                               const double* x, const double* k, const double* z, double* out,
                               double* err, cudaStream_t st);
 
+static int lu_plan_of(pjg_mech* m, void** plan)
+{
+    std::lock_guard<std::mutex> g(m->lock);
+    if (!m->lu_plan) {
+        int rc = pjg_internal_lu_plan_create(m->nn, m->crs_ptr.data(), m->crs_ind.data(), &m->lu_plan);
+        if (rc) return rc;
+    }
+    *plan = m->lu_plan;
+    return 0;
+}
+
+int pjg_lu_plan_info(pjg_mech* m, int32_t* perm, int32_t* nnz_lu, int64_t* fma)
+{
+    if (!m) return fail(PJG_ERR_ARG, "null mechanism");
+    void* pl = nullptr;
+    if (int rc = lu_plan_of(m, &pl)) return rc;
+    pjg_internal_lu_plan_info(pl, perm, nnz_lu, fma);
+    return 0;
+}
+
+int pjg_lu_factor_sparse(pjg_mech* m, int64_t n, char order, double s, const double* h, double h0,
+                         const double* jac, double* lu, int32_t* info, void* stream)
+{
+    if (!m) return fail(PJG_ERR_ARG, "null mechanism");
+    void* pl = nullptr;
+    if (int rc = lu_plan_of(m, &pl)) return rc;
+    return pjg_internal_lu_factor_sparse(pl, n, order, s, h, h0, jac, lu, info, (cudaStream_t)stream);
+}
+
+int pjg_lu_solve_sparse(pjg_mech* m, int64_t n, char order, const double* lu, double* b, void* stream)
+{
+    if (!m) return fail(PJG_ERR_ARG, "null mechanism");
+    void* pl = nullptr;
+    if (int rc = lu_plan_of(m, &pl)) return rc;
+    return pjg_internal_lu_solve_sparse(pl, n, order, lu, b, (cudaStream_t)stream);
+}
+
 // One step of ROS2 (Verwer, Spee, Blom and Hundsdorfer, SIAM J. Sci. Comput.
 // 20(4), 1999), gamma = 1 + 1/sqrt(2):
 //   (I - gamma h J) k1 = f(y),  (I - gamma h J) k2 = f(y + h k1) - 2 k1,
 //   y_new = y + 1.5 h k1 + 0.5 h k2,  err = y_new - (y + h k1) = 0.5 h (k1 + k2),
-// with J the analytical Jacobian at y and f the species rates.
+// with J the analytical Jacobian at y and f the species rates.  lu_kind 0
+// factors with partial pivoting, 1 with the mechanism's static-pivot sparse
+// plan (piv_work unused).
 int pjg_ros2_step(pjg_mech* m, int64_t n, char order, int conp, const double* param,
-                  const double* phi, const double* h, double h0, double* phi_new, double* err,
-                  double* jac_work, int32_t* piv_work, double* vec_work, int32_t* info,
+                  const double* phi, const double* h, double h0, int lu_kind, double* phi_new,
+                  double* err, double* jac_work, int32_t* piv_work, double* vec_work, int32_t* info,
                   void* stream)
 {
     if (!m) return fail(PJG_ERR_ARG, "null mechanism");
     if (n < 0) return fail(PJG_ERR_ARG, "negative problem size");
+    if (lu_kind != 0 && lu_kind != 1) return fail(PJG_ERR_ARG, "lu_kind must be 0 or 1");
     if (n == 0) return 0;
-    if (!phi || !param || !phi_new || !jac_work || !piv_work || !vec_work)
+    if (!phi || !param || !phi_new || !jac_work || !vec_work || (lu_kind == 0 && !piv_work))
         return fail(PJG_ERR_ARG, "null array");
     if (phi_new == phi) return fail(PJG_ERR_ARG, "phi_new must not alias phi");
     const cudaStream_t st = (cudaStream_t)stream;
     const int nn = m->nn;
     const double gamma = 1.7071067811865475;  // 1 + 1/sqrt(2)
+    void* plan = nullptr;
+    if (lu_kind == 1)
+        if (int rc = lu_plan_of(m, &plan)) return rc;
+    auto factor = [&]() {
+        return lu_kind == 0
+                   ? pjg_internal_lu_factor(nn, n, order, gamma, h, h0, jac_work, jac_work, piv_work, info, st)
+                   : pjg_internal_lu_factor_sparse(plan, n, order, gamma, h, h0, jac_work, jac_work, info, st);
+    };
+    auto solve = [&](double* b) {
+        return lu_kind == 0 ? pjg_internal_lu_solve(nn, n, order, jac_work, piv_work, b, st)
+                            : pjg_internal_lu_solve_sparse(plan, n, order, jac_work, b, st);
+    };
     double* k1 = vec_work;
     double* k2 = vec_work + (size_t)n * nn;
     int rc = run_eval(m, PJG_SPECIES_RATES, n, order, conp, 0, param, phi, k1, st);
     if (!rc) rc = run_eval(m, PJG_JACOBIAN, n, order, conp, PJG_JAC_FULL, param, phi, jac_work, st);
-    if (!rc) rc = pjg_internal_lu_factor(nn, n, order, gamma, h, h0, jac_work, jac_work, piv_work, info, st);
-    if (!rc) rc = pjg_internal_lu_solve(nn, n, order, jac_work, piv_work, k1, st);
+    if (!rc) rc = factor();
+    if (!rc) rc = solve(k1);
     if (!rc) rc = pjg_internal_ros2_combine(0, nn, n, order, h, h0, phi, k1, nullptr, phi_new, nullptr, st);
     if (!rc) rc = run_eval(m, PJG_SPECIES_RATES, n, order, conp, 0, param, phi_new, k2, st);
     if (!rc) rc = pjg_internal_ros2_combine(1, nn, n, order, h, h0, k2, k1, nullptr, k2, nullptr, st);
-    if (!rc) rc = pjg_internal_lu_solve(nn, n, order, jac_work, piv_work, k2, st);
+    if (!rc) rc = solve(k2);
     if (!rc) rc = pjg_internal_ros2_combine(2, nn, n, order, h, h0, phi, k1, k2, phi_new, err, st);
     return rc;
 }

@@ -21,6 +21,7 @@
 
 #include <cfloat>
 #include <cstdint>
+#include <vector>
 
 #include "../../include/pyjac_gb300.h"
 
@@ -200,6 +201,153 @@ __global__ void __launch_bounds__(LU_THREADS, LU_MINB) lu_factor_kernel(int nn, 
     }
 }
 
+// ---- Static-pivot sparse LU (no row interchanges), the factorisation of
+// implicit chemistry solvers such as KPP: rows and columns are ordered once,
+// on the host, by the Markowitz rule on the Jacobian's pattern, and step k
+// updates only the structural rows R_k x columns C_k of the filled pattern.
+// The matrix of a state stays dense in shared memory in the permuted order,
+// so no position lookups are needed; GRI-Mech 3.0 takes 19,752 FMAs per state
+// against 51,039 for the dense factorisation.
+//
+// Plan tables (int32, one device array): perm[nn] (permuted position ->
+// variable), then the offsets roff, coff, loff, uoff [nn + 1 each] into the
+// index lists ridx (R_k), cidx (C_k), lidx (columns c < r of L's row r),
+// uidx (columns c > r of U's row r).
+struct LuPlanView {
+    int nn;
+    const int *perm, *roff, *coff, *loff, *uoff, *ridx, *cidx, *lidx, *uidx;
+};
+
+// S consecutive states per block (4, or 2 or 1 where four matrices do not fit
+// in shared memory), eliminated in lockstep by 32 S threads: in loads,
+// stores and scalings each thread serves one state, so F-order loads cover
+// whole 32-byte sectors; in the update each thread takes one pattern position
+// for all S states, so one index lookup and one barrier pair serve S states.
+constexpr int kLusMaxStates = 4;
+
+template <bool F, int S>
+__global__ void __launch_bounds__(32 * S) lu_sparse_kernel(long long n, double s,
+                                                           const double* __restrict__ h, double h0,
+                                                           const double* jac, double* lu,
+                                                           int32_t* __restrict__ info, LuPlanView pl)
+{
+    extern __shared__ double smem[];
+    __shared__ double gst[S];
+    __shared__ int fz[S];
+    constexpr int T = 32 * S, TS = 32;
+    const int nn = pl.nn;
+    const int tid = threadIdx.x;
+    const int pitch = nn | 1;
+    const int msz = nn * pitch;
+    const int nsq = nn * nn;
+    const int my = tid % S;   // this thread's state slot in loads, stores and scalings
+    const int lane_s = tid / S;
+    double* A = smem + (size_t)my * msz;
+    const long long ngroups = (n + S - 1) / S;
+    for (long long grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        const long long i0 = grp * S;
+        const int here = (int)((n - i0) < S ? (n - i0) : S);
+        if (tid < S) {
+            gst[tid] = tid < here ? s * (h ? h[i0 + tid] : h0) : 0.0;
+            fz[tid] = 0;
+        }
+        __syncthreads();
+        {
+            const double g = gst[my];
+            const bool live = my < here;
+            Cursor cu(lane_s, TS, nn);
+            for (int e = lane_s; e < nsq; e += TS) {
+                const double j = live ? jac[mat_idx(F, i0 + my, n, nn, __ldg(pl.perm + cu.r),
+                                                    __ldg(pl.perm + cu.c))]
+                                      : 0.0;
+                A[cu.r * pitch + cu.c] = fma(-g, j, cu.r == cu.c ? 1.0 : 0.0);
+                cu.next();
+            }
+        }
+        __syncthreads();
+        for (int k = 0; k < nn; ++k) {
+            const int r0 = __ldg(pl.roff + k), nr = __ldg(pl.roff + k + 1) - r0;
+            if (tid < S && smem[(size_t)tid * msz + k * pitch + k] == 0.0 && !fz[tid]) fz[tid] = k + 1;
+            if (nr == 0) continue;  // nothing below the pivot: no update, no barrier
+            const int c0 = __ldg(pl.coff + k), nc = __ldg(pl.coff + k + 1) - c0;
+            const int* R = pl.ridx + r0;
+            const int* C = pl.cidx + c0;
+            if (lane_s < nr) {
+                const double p = A[k * pitch + k];
+                if (p != 0.0) {
+                    const bool recip = fabs(p) >= DBL_MIN;
+                    const double inv = recip ? __drcp_rn(p) : 0.0;
+                    for (int q = lane_s; q < nr; q += TS) {
+                        double* x = A + __ldg(R + q) * pitch + k;
+                        *x = recip ? *x * inv : *x / p;
+                    }
+                }
+            }
+            __syncthreads();
+            const int mm = nr * nc;
+            if (tid < mm) {
+                Cursor cu(tid, T, nc);
+                for (int e = tid; e < mm; e += T) {
+                    const int r = __ldg(R + cu.r), c = __ldg(C + cu.c);
+                    const int o = r * pitch + c, ol = r * pitch + k, ou = k * pitch + c;
+                    double l[S], u[S], v[S];
+#pragma unroll
+                    for (int q = 0; q < S; ++q) {
+                        const double* B = smem + (size_t)q * msz;
+                        l[q] = B[ol];
+                        u[q] = B[ou];
+                        v[q] = B[o];
+                    }
+#pragma unroll
+                    for (int q = 0; q < S; ++q) smem[(size_t)q * msz + o] = fma(-l[q], u[q], v[q]);
+                    cu.next();
+                }
+            }
+            __syncthreads();
+        }
+        if (my < here) {
+            Cursor cu(lane_s, TS, nn);
+            for (int e = lane_s; e < nsq; e += TS) {
+                lu[mat_idx(F, i0 + my, n, nn, cu.r, cu.c)] = A[cu.r * pitch + cu.c];
+                cu.next();
+            }
+        }
+        if (tid < here && info) info[i0 + tid] = fz[tid];
+        __syncthreads();
+    }
+}
+
+// one thread per state: y = P b, L y = y and U x = y over the filled pattern
+// only (row-oriented FMA dot products in increasing column order), x back to
+// the variables' order
+template <bool F>
+__global__ void __launch_bounds__(128) lu_sparse_solve_kernel(long long n, const double* __restrict__ lu,
+                                                              double* b, LuPlanView pl)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int nn = pl.nn;
+    double y[kSolveNMax];
+    for (int r = 0; r < nn; ++r) y[r] = b[vec_idx(F, i, n, nn, __ldg(pl.perm + r))];
+    for (int r = 1; r < nn; ++r) {
+        double acc = y[r];
+        for (int q = __ldg(pl.loff + r); q < __ldg(pl.loff + r + 1); ++q) {
+            const int c = __ldg(pl.lidx + q);
+            acc = fma(-__ldg(lu + mat_idx(F, i, n, nn, r, c)), y[c], acc);
+        }
+        y[r] = acc;
+    }
+    for (int r = nn - 1; r >= 0; --r) {
+        double acc = y[r];
+        for (int q = __ldg(pl.uoff + r); q < __ldg(pl.uoff + r + 1); ++q) {
+            const int c = __ldg(pl.uidx + q);
+            acc = fma(-__ldg(lu + mat_idx(F, i, n, nn, r, c)), y[c], acc);
+        }
+        y[r] = acc / __ldg(lu + mat_idx(F, i, n, nn, r, r));
+    }
+    for (int r = 0; r < nn; ++r) b[vec_idx(F, i, n, nn, __ldg(pl.perm + r))] = y[r];
+}
+
 // one thread per state: row interchanges, unit-lower then upper substitution
 // (row-oriented: each y_r accumulates its dot product in increasing column
 // order by FMA, and the upper rows divide by the diagonal)
@@ -284,6 +432,127 @@ int lu_factor_config(int nn, size_t* smem, int* grid)
     return 0;
 }
 
+
+// ---- host side of the static-pivot plan
+
+// Markowitz order of a square pattern (row-major bytes, diagonal included):
+// at each step the remaining diagonal entry with the least
+// (row count - 1) x (column count - 1) over the remaining submatrix, the
+// lowest index on ties; the pattern fills in as the step eliminates.
+static void markowitz_order(int nn, std::vector<char> A, std::vector<int>& perm)
+{
+    std::vector<char> done(nn, 0);
+    perm.clear();
+    for (int step = 0; step < nn; ++step) {
+        int best = -1;
+        long long bscore = 0;
+        for (int v = 0; v < nn; ++v) {
+            if (done[v]) continue;
+            long long rc = 0, cc = 0;
+            for (int j = 0; j < nn; ++j)
+                if (!done[j] && j != v) {
+                    rc += A[(size_t)v * nn + j];
+                    cc += A[(size_t)j * nn + v];
+                }
+            const long long sc = rc * cc;
+            if (best < 0 || sc < bscore) {
+                best = v;
+                bscore = sc;
+            }
+        }
+        for (int r = 0; r < nn; ++r) {
+            if (done[r] || r == best || !A[(size_t)r * nn + best]) continue;
+            for (int c = 0; c < nn; ++c)
+                if (!done[c] && c != best && A[(size_t)best * nn + c]) A[(size_t)r * nn + c] = 1;
+        }
+        done[best] = 1;
+        perm.push_back(best);
+    }
+}
+
+struct LuPlan {
+    int nn = 0;
+    int* d = nullptr;  // device tables
+    LuPlanView view{};
+    std::vector<int> perm;
+    long long fma = 0;
+    int nnz_lu = 0;
+};
+
+// pattern of M = I - s h J from the Jacobian's CRS pattern (C order rows)
+static int build_plan_tables(int nn, const int* row_ptr, const int* col_ind, std::vector<int>& perm,
+                             std::vector<int>& tab, long long* fma, int* nnz_lu)
+{
+    std::vector<char> A((size_t)nn * nn, 0);
+    for (int r = 0; r < nn; ++r) {
+        A[(size_t)r * nn + r] = 1;
+        for (int q = row_ptr[r]; q < row_ptr[r + 1]; ++q) {
+            const int c = col_ind[q];
+            if (c < 0 || c >= nn) return PJG_ERR_ARG;
+            A[(size_t)r * nn + c] = 1;
+        }
+    }
+    markowitz_order(nn, A, perm);
+    std::vector<char> B((size_t)nn * nn);
+    for (int r = 0; r < nn; ++r)
+        for (int c = 0; c < nn; ++c) B[(size_t)r * nn + c] = A[(size_t)perm[r] * nn + perm[c]];
+    std::vector<int> roff(1, 0), coff(1, 0), ridx, cidx;
+    *fma = 0;
+    for (int k = 0; k < nn; ++k) {
+        const size_t r_before = ridx.size(), c_before = cidx.size();
+        for (int r = k + 1; r < nn; ++r)
+            if (B[(size_t)r * nn + k]) ridx.push_back(r);
+        for (int c = k + 1; c < nn; ++c)
+            if (B[(size_t)k * nn + c]) cidx.push_back(c);
+        for (size_t a = r_before; a < ridx.size(); ++a)
+            for (size_t b = c_before; b < cidx.size(); ++b) B[(size_t)ridx[a] * nn + cidx[b]] = 1;
+        *fma += (long long)(ridx.size() - r_before) * (long long)(cidx.size() - c_before);
+        roff.push_back((int)ridx.size());
+        coff.push_back((int)cidx.size());
+    }
+    std::vector<int> loff(1, 0), uoff(1, 0), lidx, uidx;
+    *nnz_lu = 0;
+    for (int r = 0; r < nn; ++r) {
+        for (int c = 0; c < nn; ++c) {
+            if (!B[(size_t)r * nn + c]) continue;
+            ++*nnz_lu;
+            if (c < r) lidx.push_back(c);
+            if (c > r) uidx.push_back(c);
+        }
+        loff.push_back((int)lidx.size());
+        uoff.push_back((int)uidx.size());
+    }
+    tab.clear();
+    tab.insert(tab.end(), perm.begin(), perm.end());
+    for (auto* v : {&roff, &coff, &loff, &uoff}) tab.insert(tab.end(), v->begin(), v->end());
+    for (auto* v : {&ridx, &cidx, &lidx, &uidx}) tab.insert(tab.end(), v->begin(), v->end());
+    tab.push_back(0);  // keeps every list's end inside the array
+    return 0;
+}
+
+template <int S>
+int lu_sparse_launch(const LuPlan* pl, long long n, char order, double s, const double* h, double h0,
+                     const double* jac, double* lu, int32_t* info, cudaStream_t st, int sms)
+{
+    const size_t smem = (size_t)S * pl->nn * (pl->nn | 1) * sizeof(double);
+    const void* fn = (const void*)lu_sparse_kernel<false, S>;
+    const void* fnF = (const void*)lu_sparse_kernel<true, S>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(fnF, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return pjg_internal_fail(PJG_ERR_CUDA, "cannot reserve shared memory for the sparse LU kernel");
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * S, smem) != cudaSuccess || per_sm < 1)
+        return pjg_internal_fail(PJG_ERR_CUDA, "sparse LU kernel does not fit on the device");
+    long long grid = (long long)sms * per_sm;
+    const long long groups = (n + S - 1) / S;
+    if (groups < grid) grid = groups;
+    if (order == 'F')
+        lu_sparse_kernel<true, S><<<(int)grid, 32 * S, smem, st>>>(n, s, h, h0, jac, lu, info, pl->view);
+    else
+        lu_sparse_kernel<false, S><<<(int)grid, 32 * S, smem, st>>>(n, s, h, h0, jac, lu, info, pl->view);
+    return 0;
+}
+
 }  // namespace
 
 extern "C" int pjg_internal_lu_factor(int32_t nn, int64_t n, char order, double s, const double* h, double h0,
@@ -339,6 +608,124 @@ extern "C" int pjg_internal_ros2_combine(int op, int32_t nn, int64_t n, char ord
         ros2_combine_kernel<false><<<grid, 256, 0, st>>>(op, nn, n, h, h0, x, k, z, out, err);
     pjg_internal_count_launch();
     if (cudaGetLastError() != cudaSuccess) return pjg_internal_fail(PJG_ERR_CUDA, "ROS2 stage launch failed");
+    return 0;
+}
+
+// static-pivot plans are owned by the mechanism (pjg_capi.cu)
+extern "C" int pjg_internal_lu_plan_create(int32_t nn, const int32_t* row_ptr, const int32_t* col_ind,
+                                           void** out)
+{
+    if (nn < 1 || nn > kLuMaxNN) return pjg_internal_fail(PJG_ERR_UNSUPPORTED, "LU: nn must be in [1, 169]");
+    LuPlan* pl = new LuPlan();
+    pl->nn = nn;
+    std::vector<int> tab;
+    if (build_plan_tables(nn, row_ptr, col_ind, pl->perm, tab, &pl->fma, &pl->nnz_lu)) {
+        delete pl;
+        return pjg_internal_fail(PJG_ERR_TABLES, "Jacobian pattern index out of range");
+    }
+    if (cudaMalloc((void**)&pl->d, tab.size() * sizeof(int)) != cudaSuccess ||
+        cudaMemcpy(pl->d, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(pl->d);
+        delete pl;
+        return pjg_internal_fail(PJG_ERR_CUDA, "cannot upload the sparse LU plan");
+    }
+    const int* d = pl->d;
+    LuPlanView& v = pl->view;
+    v.nn = nn;
+    v.perm = d;
+    v.roff = d + nn;
+    v.coff = v.roff + nn + 1;
+    v.loff = v.coff + nn + 1;
+    v.uoff = v.loff + nn + 1;
+    v.ridx = v.uoff + nn + 1;
+    v.cidx = v.ridx + tab[2 * nn];      // + roff[nn]
+    v.lidx = v.cidx + tab[3 * nn + 1];  // + coff[nn]
+    v.uidx = v.lidx + tab[4 * nn + 2];  // + loff[nn]
+    *out = pl;
+    return 0;
+}
+
+extern "C" void pjg_internal_lu_plan_destroy(void* p)
+{
+    LuPlan* pl = static_cast<LuPlan*>(p);
+    if (!pl) return;
+    cudaFree(pl->d);
+    delete pl;
+}
+
+extern "C" void pjg_internal_lu_plan_info(const void* p, int32_t* perm, int32_t* nnz_lu, int64_t* fma)
+{
+    const LuPlan* pl = static_cast<const LuPlan*>(p);
+    if (perm)
+        for (int k = 0; k < pl->nn; ++k) perm[k] = pl->perm[k];
+    if (nnz_lu) *nnz_lu = pl->nnz_lu;
+    if (fma) *fma = pl->fma;
+}
+
+extern "C" int pjg_internal_lu_factor_sparse(const void* p, int64_t n, char order, double s, const double* h,
+                                             double h0, const double* jac, double* lu, int32_t* info,
+                                             cudaStream_t st)
+{
+    const LuPlan* pl = static_cast<const LuPlan*>(p);
+    if (n < 0) return pjg_internal_fail(PJG_ERR_ARG, "negative problem size");
+    if (order != 'C' && order != 'F') return pjg_internal_fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
+    if (n == 0) return 0;
+    if (!jac || !lu) return pjg_internal_fail(PJG_ERR_ARG, "null array");
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return pjg_internal_fail(PJG_ERR_CUDA, "device query failed");
+    }
+    const size_t per_state = (size_t)pl->nn * (pl->nn | 1) * sizeof(double);
+    const size_t limit = (227u << 10) - 64;  // opt-in shared memory of one block, less the static part
+    int rc;
+    if (kLusMaxStates * per_state <= limit)
+        rc = lu_sparse_launch<kLusMaxStates>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
+    else if (2 * per_state <= limit)
+        rc = lu_sparse_launch<2>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
+    else
+        rc = lu_sparse_launch<1>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
+    if (rc) return rc;
+    pjg_internal_count_launch();
+    if (cudaGetLastError() != cudaSuccess) return pjg_internal_fail(PJG_ERR_CUDA, "sparse LU launch failed");
+    return 0;
+}
+
+extern "C" int pjg_internal_lu_solve_sparse(const void* p, int64_t n, char order, const double* lu, double* b,
+                                            cudaStream_t st)
+{
+    const LuPlan* pl = static_cast<const LuPlan*>(p);
+    if (n < 0) return pjg_internal_fail(PJG_ERR_ARG, "negative problem size");
+    if (order != 'C' && order != 'F') return pjg_internal_fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
+    if (n == 0) return 0;
+    if (!lu || !b) return pjg_internal_fail(PJG_ERR_ARG, "null array");
+    const int grid = (int)((n + 127) / 128);
+    if (order == 'F')
+        lu_sparse_solve_kernel<true><<<grid, 128, 0, st>>>(n, lu, b, pl->view);
+    else
+        lu_sparse_solve_kernel<false><<<grid, 128, 0, st>>>(n, lu, b, pl->view);
+    pjg_internal_count_launch();
+    if (cudaGetLastError() != cudaSuccess) return pjg_internal_fail(PJG_ERR_CUDA, "sparse LU solve launch failed");
+    return 0;
+}
+
+// host only: the Markowitz order and the counts of a pattern (no device work)
+extern "C" int pjg_lu_symbolic(int32_t nn, const int32_t* row_ptr, const int32_t* col_ind, int32_t* perm,
+                               int32_t* nnz_lu, int64_t* fma)
+{
+    if (nn < 1 || nn > kLuMaxNN) return pjg_internal_fail(PJG_ERR_UNSUPPORTED, "LU: nn must be in [1, 169]");
+    if (!row_ptr || !col_ind) return pjg_internal_fail(PJG_ERR_ARG, "null array");
+    std::vector<int> pv, tab;
+    long long f = 0;
+    int z = 0;
+    if (build_plan_tables(nn, row_ptr, col_ind, pv, tab, &f, &z))
+        return pjg_internal_fail(PJG_ERR_ARG, "pattern index out of range");
+    if (perm)
+        for (int k = 0; k < nn; ++k) perm[k] = pv[k];
+    if (nnz_lu) *nnz_lu = z;
+    if (fma) *fma = f;
     return 0;
 }
 

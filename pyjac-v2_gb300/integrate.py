@@ -4,7 +4,14 @@ The consumer of the Jacobian in real use: an implicit ODE solver factors the
 Newton matrix M = I - s h J of every state and solves with it once per stage.
 No reference counterpart (the reference lists coupling to Rosenbrock solvers
 as future work).  Everything runs in the CUDA library (include/pyjac_gb300.h:
-pjg_lu_factor, pjg_lu_solve, pjg_ros2_step) on the current torch stream.
+pjg_lu_factor, pjg_lu_solve, pjg_lu_factor_sparse, pjg_lu_solve_sparse,
+pjg_ros2_step) on the current torch stream.
+
+Two factorisations: partial pivoting (LAPACK dgetf2's algorithm, any dense
+matrix up to 169 x 169), and the static-pivot sparse LU of implicit chemistry
+solvers (KPP): rows and columns ordered once by the Markowitz rule on the
+mechanism's Jacobian pattern, no interchanges, only the filled pattern
+updated (GRI-Mech 3.0: 19,752 FMAs per state instead of 51,039).
 
 Layouts are the dense Jacobian's: order 'C' — jac and lu (N, NN, NN)
 [state, row, col]; order 'F' — (NN, NN, N) [col, row, state].  Vectors and
@@ -80,6 +87,66 @@ def lu_solve(lu, piv, b, order="C"):
     return b
 
 
+def lu_symbolic(row_ptr, col_ind):
+    """Markowitz order of a CRS pattern (plus the diagonal) and its counts,
+    computed on the host: (perm, nnz of L + U, FMAs per state), with
+    perm[position] = variable."""
+    import ctypes
+    import numpy as np
+    rp = np.ascontiguousarray(row_ptr, dtype=np.int32)
+    ci = np.ascontiguousarray(col_ind, dtype=np.int32)
+    nn = rp.size - 1
+    perm = np.empty(nn, dtype=np.int32)
+    nnz = ctypes.c_int32()
+    fma = ctypes.c_int64()
+    _lib.check("pjg_lu_symbolic", _lib.load().pjg_lu_symbolic(
+        nn, rp.ctypes.data, ci.ctypes.data, perm.ctypes.data, ctypes.addressof(nnz),
+        ctypes.byref(fma)))
+    return perm, nnz.value, fma.value
+
+
+def lu_plan_info(evaluator):
+    """The mechanism's static-pivot plan: (perm, nnz of L + U, FMAs per state)."""
+    import ctypes
+    import numpy as np
+    perm = np.empty(evaluator.nn, dtype=np.int32)
+    nnz = ctypes.c_int32()
+    fma = ctypes.c_int64()
+    _lib.check("pjg_lu_plan_info", evaluator._lib.pjg_lu_plan_info(
+        evaluator.handle, perm.ctypes.data, ctypes.addressof(nnz), ctypes.byref(fma)))
+    return perm, nnz.value, fma.value
+
+
+def lu_factor_sparse(evaluator, jac, h, s=1.0, order="C", out=None):
+    """Static-pivot factorisation of M_i = I - s h_i J_i on the evaluator's
+    mechanism plan.  Returns (lu, info): lu like jac, holding the factors of
+    the permuted matrix M[perm][:, perm]; info int32 (N,) = 0 or the 1-based
+    step of the first exactly zero pivot."""
+    _check_f64(jac)
+    n, nn = _n_of(jac, order)
+    if nn != evaluator.nn:
+        raise ValueError("jac does not match the mechanism")
+    lu = torch.empty_like(jac) if out is None else out
+    _check_f64(lu)
+    inf = torch.empty(n, dtype=torch.int32, device=jac.device)
+    hp, h0 = _h_args(h, n)
+    _lib.check("pjg_lu_factor_sparse", evaluator._lib.pjg_lu_factor_sparse(
+        evaluator.handle, n, _order(order), float(s), hp, h0, jac.data_ptr(), lu.data_ptr(),
+        inf.data_ptr(), _stream(jac)))
+    return lu, inf
+
+
+def lu_solve_sparse(evaluator, lu, b, order="C"):
+    """b <- M^-1 b in place from lu_factor_sparse's output; returns b."""
+    _check_f64(lu, b)
+    n, nn = _n_of(lu, order)
+    if b.numel() != n * nn:
+        raise ValueError("b must hold N x NN values")
+    _lib.check("pjg_lu_solve_sparse", evaluator._lib.pjg_lu_solve_sparse(
+        evaluator.handle, n, _order(order), lu.data_ptr(), b.data_ptr(), _stream(lu)))
+    return b
+
+
 class Ros2Stepper(object):
     """Steps of the L-stable two-stage Rosenbrock method ROS2 (Verwer, Spee,
     Blom and Hundsdorfer, SIAM J. Sci. Comput. 20(4), 1999) for up to
@@ -89,13 +156,18 @@ class Ros2Stepper(object):
         y_new = y + 1.5 h k1 + 0.5 h k2,  err = 0.5 h (k1 + k2)
 
     with f the species rates and J the analytical Jacobian at y
-    (gamma = 1 + 1/sqrt 2).  The work arrays (a dense Jacobian per state) are
-    allocated once; after a step ``lu`` and ``piv`` hold the factors of the
-    step's Newton matrix."""
+    (gamma = 1 + 1/sqrt 2).  ``lu_kind`` "pivoting" factors the Newton matrix
+    with partial pivoting, "sparse" with the mechanism's static-pivot plan.
+    The work arrays (a dense Jacobian per state) are allocated once; after a
+    step ``lu`` (and ``piv`` for "pivoting") hold the factors of the step's
+    Newton matrix."""
 
-    def __init__(self, evaluator, capacity, order="C", device=None):
+    def __init__(self, evaluator, capacity, order="C", device=None, lu_kind="pivoting"):
+        if lu_kind not in ("pivoting", "sparse"):
+            raise ValueError("lu_kind must be 'pivoting' or 'sparse'")
         self.ev = evaluator
         self.order = order
+        self.lu_kind = lu_kind
         self.capacity = int(capacity)
         nn = evaluator.nn
         dev = device or torch.device("cuda", torch.cuda.current_device())
@@ -118,6 +190,7 @@ class Ros2Stepper(object):
         hp, h0 = _h_args(h, n)
         _lib.check("pjg_ros2_step", self.ev._lib.pjg_ros2_step(
             self.ev.handle, n, _order(self.order), int(bool(conp)), param.data_ptr(), phi.data_ptr(),
-            hp, h0, out.data_ptr(), err.data_ptr(), self.lu.data_ptr(), self.piv.data_ptr(),
+            hp, h0, 0 if self.lu_kind == "pivoting" else 1, out.data_ptr(), err.data_ptr(),
+            self.lu.data_ptr(), self.piv.data_ptr(),
             self.vec.data_ptr(), self.info.data_ptr(), st))
         return out, err, self.info[:n]

@@ -144,12 +144,12 @@ def generate(n_species=500, n_reactions=2500, seed=0, frac_thd=0.10, frac_troe=0
     thermo.append(n2)
     body = "\n".join(lines) + "\n" + "".join(thermo) + "END\n"
 
-    kinds = rng.permutation(
-        ["thd"] * int(round(frac_thd * n_reactions)) + ["troe"] * int(round(frac_troe * n_reactions)) +
-        ["sri"] * int(round(frac_sri * n_reactions)) + ["plog"] * int(round(frac_plog * n_reactions)) +
-        ["cheb"] * int(round(frac_cheb * n_reactions)) +
-        ["el"] * max(0, n_reactions - int(round((frac_thd + frac_troe + frac_sri + frac_plog + frac_cheb)
-                                               * n_reactions))))[:n_reactions]
+    special = (["thd"] * int(round(frac_thd * n_reactions)) +
+               ["troe"] * int(round(frac_troe * n_reactions)) +
+               ["sri"] * int(round(frac_sri * n_reactions)) +
+               ["plog"] * int(round(frac_plog * n_reactions)) +
+               ["cheb"] * int(round(frac_cheb * n_reactions)))
+    kinds = rng.permutation(special + ["el"] * max(0, n_reactions - len(special)))[:n_reactions]
     rx = ["REACTIONS"]
     made = 0
     guard = 0

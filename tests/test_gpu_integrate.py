@@ -1,11 +1,14 @@
-"""GPU Newton-matrix LU, solves and ROS2 steps against the oracle.
+"""GPU Newton-matrix LU (partial pivoting and static-pivot sparse), solves
+and ROS2 steps against the oracle.
 
-The factorisation and the solves perform the oracle's IEEE operations in the
-same order (fma entries, first-largest pivot, reciprocal scaling, rank-1 FMA
-updates; row-oriented FMA substitution), so their results must be identical
-bit for bit.  A ROS2 step also involves the rates and the Jacobian, which
-agree with the oracle to 1e-10 / 1e-8; the step is compared at 1e-9 of each
-component's scale.
+The factorisations and the solves perform the oracle's IEEE operations in the
+same order (fma entries, first-largest pivot or the static Markowitz order,
+reciprocal scaling, rank-1 FMA updates; row-oriented FMA substitution), so
+their results must be identical bit for bit.  A ROS2 step also involves the
+rates and the Jacobian: it is compared bit for bit with the oracle's
+factorisation, solves and stage arithmetic applied to this library's own
+rates and Jacobian, and within a conditioning-aware bound with the step
+computed entirely by the oracle.
 """
 import numpy as np
 import pytest
@@ -191,3 +194,121 @@ def test_ros2_trajectory_premix(cuda_device):
     y = y.cpu().numpy()
     scale = np.abs(y_ref) + 1e-8 * np.abs(y_ref).max()
     assert (np.abs(y - y_ref) / scale).max() < 1e-8
+
+
+def _plan(mech):
+    pk = pkg("pack").PackedTables(mech)
+    return oracle_mod().lu_plan(pk.crs_row_ptr, pk.crs_col_ind)
+
+
+@pytest.mark.parametrize("order", ["C", "F"])
+@pytest.mark.parametrize("name", ["h2o2", "gri30", "testmech"])
+@pytest.mark.parametrize("per_state_h", [False, True])
+def test_lu_factor_sparse_bitwise(cuda_device, order, name, per_state_h):
+    import torch
+    orc = oracle_mod()
+    integ = pkg("integrate")
+    mech, P, phi, J = _newton_inputs(name, 700, 23)
+    plan = _plan(mech)
+    h = 10.0 ** np.random.default_rng(4).uniform(-9, -3, J.shape[0]) if per_state_h else 2e-6
+    lu_ref, info_ref = orc.lu_factor_sparse(J, integ.ROS2_GAMMA, h, plan)
+    ev = pkg("api").Evaluator(mech)
+    assert np.array_equal(integ.lu_plan_info(ev)[0], plan["perm"])
+    hd = torch.from_numpy(h).to(cuda_device) if per_state_h else h
+    lu, info = integ.lu_factor_sparse(ev, _to_dev_mat(J, order, cuda_device), hd,
+                                      s=integ.ROS2_GAMMA, order=order)
+    assert np.array_equal(_from_dev_mat(lu, order), lu_ref)
+    assert np.array_equal(info.cpu().numpy(), info_ref)
+    b = np.random.default_rng(9).standard_normal((700, mech.nn))
+    x_ref = orc.lu_solve_sparse(lu_ref, b, plan)
+    x = integ.lu_solve_sparse(ev, lu, _to_dev_vec(b, order, cuda_device), order=order)
+    assert np.array_equal(_from_dev_vec(x, order), x_ref)
+
+
+def test_lu_factor_sparse_zero_pivot_info(cuda_device):
+    """A state whose Newton matrix is exactly zero (s h = 1, J = I) reports
+    info = 1, as the oracle does."""
+    import torch
+    orc = oracle_mod()
+    integ = pkg("integrate")
+    mech = load_mech("h2o2")
+    plan = _plan(mech)
+    J = np.zeros((3, mech.nn, mech.nn))
+    J[1] = np.eye(mech.nn)
+    lu_ref, info_ref = orc.lu_factor_sparse(J, 1.0, 1.0, plan)
+    ev = pkg("api").Evaluator(mech)
+    lu, info = integ.lu_factor_sparse(ev, _to_dev_mat(J, "C", cuda_device), 1.0)
+    assert list(info.cpu().numpy()) == list(info_ref) == [0, 1, 0]
+    assert np.array_equal(lu.cpu().numpy(), lu_ref)
+
+
+@pytest.mark.parametrize("order", ["C", "F"])
+@pytest.mark.parametrize("name", ["h2o2", "gri30"])
+def test_ros2_step_sparse_lu_bitwise(cuda_device, order, name):
+    """ROS2 with the static-pivot factorisation equals the oracle's sparse LU,
+    solves and stage arithmetic applied to this library's rates and Jacobian,
+    bit for bit."""
+    import torch
+    orc = oracle_mod()
+    integ = pkg("integrate")
+    mech = load_mech(name)
+    plan = _plan(mech)
+    n = 257
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=19, x_floor=1e-12)
+    h = 10.0 ** np.random.default_rng(2).uniform(-10, -7, n)
+    ev = pkg("api").Evaluator(mech)
+    Pd, hd = torch.from_numpy(P).to(cuda_device), torch.from_numpy(h).to(cuda_device)
+    phid = _to_dev_vec(phi, order, cuda_device)
+
+    def rates(y):
+        return _from_dev_vec(ev.species_rates(Pd, _to_dev_vec(y, order, cuda_device), order=order),
+                             order)
+
+    J = _from_dev_mat(ev.jacobian(Pd, phid, order=order), order)
+    lu, info_ref = orc.lu_factor_sparse(J, integ.ROS2_GAMMA, h, plan)
+    k1 = orc.lu_solve_sparse(lu, rates(phi), plan)
+    k2 = orc.lu_solve_sparse(lu, orc.ros2_combine(1, h, rates(orc.ros2_combine(0, h, phi, k1)), k1),
+                             plan)
+    ref, err_ref = orc.ros2_combine(2, h, phi, k1, k2)
+    st = integ.Ros2Stepper(ev, n, order=order, lu_kind="sparse")
+    out, err, info = st.step(Pd, phid, hd)
+    assert np.array_equal(info.cpu().numpy(), info_ref)
+    assert np.array_equal(_from_dev_vec(out, order), ref)
+    assert np.array_equal(_from_dev_vec(err, order), err_ref)
+
+
+@pytest.mark.parametrize("n_species,states_per_block", [(119, 2), (168, 1)])
+def test_lu_factor_sparse_large_mechanisms(cuda_device, tmp_path, n_species, states_per_block):
+    """Seeded synthetic mechanisms whose Newton matrices (NN = 120, 169) fit two
+    or one per block of shared memory: the sparse and the pivoting
+    factorisations stay bit for bit the oracle's.  The random mechanisms'
+    Jacobians reach 1e168 at these states, where elimination without
+    interchanges overflows, so each state's Jacobian is divided by its largest
+    entry first (M = I - 0.0171 J / max|J|); results are compared as bit
+    patterns."""
+    import torch
+    orc = oracle_mod()
+    integ = pkg("integrate")
+    path = str(tmp_path / "syn.inp")
+    pkg("mech.synthetic").write(path, n_species=n_species, n_reactions=3 * n_species, seed=5)
+    mech = pkg().load_mechanism(path)
+    assert mech.nn == n_species + 1
+    assert 4 * mech.nn * (mech.nn | 1) * 8 > 227 * 1024  # not the four-state path
+    n = 37
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=6, x_floor=1e-12)
+    J = orc.Oracle(mech).jacobian(P, phi)
+    J = J / np.abs(J).max(axis=(1, 2), keepdims=True)
+    bits = lambda a: np.ascontiguousarray(a).view(np.int64)
+    plan = _plan(mech)
+    lu_ref, info_ref = orc.lu_factor_sparse(J, integ.ROS2_GAMMA, 1e-2, plan)
+    assert np.isfinite(lu_ref).all() and (info_ref == 0).all()
+    ev = pkg("api").Evaluator(mech)
+    for order in ("C", "F"):
+        lu, info = integ.lu_factor_sparse(ev, _to_dev_mat(J, order, cuda_device), 1e-2,
+                                          s=integ.ROS2_GAMMA, order=order)
+        assert np.array_equal(bits(_from_dev_mat(lu, order)), bits(lu_ref))
+        assert np.array_equal(info.cpu().numpy(), info_ref)
+    lu_d, piv_d, _ = integ.lu_factor(_to_dev_mat(J, "C", cuda_device), 1e-2, s=integ.ROS2_GAMMA)
+    lu_p, piv_p, _ = orc.lu_factor(J, integ.ROS2_GAMMA, 1e-2)
+    assert np.array_equal(bits(lu_d.cpu().numpy()), bits(lu_p))
+    assert np.array_equal(piv_d.cpu().numpy(), piv_p)

@@ -122,3 +122,68 @@ def test_ros2_converges_at_second_order():
         errs.append((np.abs(y[0] - ref) / scale).max())
     rates = [errs[i] / errs[i + 1] for i in range(2)]
     assert all(3.0 < r < 5.5 for r in rates), (errs, rates)
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30", "testmech"])
+def test_lu_symbolic_matches_oracle_plan(name):
+    """The library's host Markowitz order (pjg_lu_symbolic, no GPU) equals the
+    oracle's independent restatement, with the same fill and FMA counts."""
+    orc = oracle_mod()
+    mech = load_mech(name)
+    pk = pkg("pack").PackedTables(mech)
+    plan = orc.lu_plan(pk.crs_row_ptr, pk.crs_col_ind)
+    perm, nnz, fma = pkg("integrate").lu_symbolic(pk.crs_row_ptr, pk.crs_col_ind)
+    assert np.array_equal(perm, plan["perm"])
+    assert (nnz, fma) == (plan["nnz_lu"], plan["fma"])
+    if name == "gri30":
+        assert (nnz, fma) == (2043, 19752)  # against 2,916 entries and 51,039 FMAs dense
+
+
+def test_lu_symbolic_random_patterns():
+    orc = oracle_mod()
+    rng = np.random.default_rng(4)
+    for nn in (1, 3, 17, 40):
+        A = rng.random((nn, nn)) < 0.2
+        rp = np.concatenate([[0], np.cumsum(A.sum(1))]).astype(np.int32)
+        ci = np.nonzero(A)[1].astype(np.int32)
+        plan = orc.lu_plan(rp, ci)
+        perm, nnz, fma = pkg("integrate").lu_symbolic(rp, ci)
+        assert np.array_equal(perm, plan["perm"]) and (nnz, fma) == (plan["nnz_lu"], plan["fma"])
+
+
+@pytest.mark.parametrize("h", [1e-8, 1e-6, 1e-4])
+def test_sparse_lu_solves_match_numpy(h):
+    orc = oracle_mod()
+    mech = load_mech("gri30")
+    pk = pkg("pack").PackedTables(mech)
+    plan = orc.lu_plan(pk.crs_row_ptr, pk.crs_col_ind)
+    P, phi = pkg("states").draw_states(mech.n_species, 64, seed=3, x_floor=1e-12)
+    J = orc.Oracle(mech).jacobian(P, phi)
+    lu, info = orc.lu_factor_sparse(J, orc.ROS2_GAMMA, h, plan)
+    assert (info == 0).all()
+    b = np.random.default_rng(1).standard_normal((64, mech.nn))
+    x = orc.lu_solve_sparse(lu, b, plan)
+    ref = np.linalg.solve(_newton(J, orc.ROS2_GAMMA, h), b[..., None])[..., 0]
+    assert (np.abs(x - ref).max(axis=1) / np.abs(ref).max(axis=1)).max() < 1e-7
+
+
+def test_ros2_sparse_lu_converges_at_second_order():
+    from scipy.integrate import solve_ivp
+    orc = oracle_mod()
+    mech, P, phi = premix_h2o2()
+    o = orc.Oracle(mech)
+    pk = pkg("pack").PackedTables(mech)
+    plan = orc.lu_plan(pk.crs_row_ptr, pk.crs_col_ind)
+    t_end = 2e-5
+    ref = solve_ivp(lambda t, y: o.species_rates(P, y[None])[0], (0, t_end), phi[0],
+                    method="Radau", jac=lambda t, y: o.jacobian(P, y[None])[0], rtol=1e-13,
+                    atol=1e-22).y[:, -1]
+    scale = np.abs(ref) + 1e-8 * np.abs(ref).max()
+    errs = []
+    for steps in (16, 32, 64):
+        y = phi.copy()
+        for _ in range(steps):
+            y, _, info = orc.ros2_step(o, P, y, t_end / steps, plan=plan)
+        errs.append((np.abs(y[0] - ref) / scale).max())
+    rates = [errs[i] / errs[i + 1] for i in range(2)]
+    assert all(3.0 < r < 5.5 for r in rates), (errs, rates)
