@@ -68,135 +68,141 @@ struct Cursor {
 constexpr long long kAbsMask = 0x7fffffffffffffffLL;
 constexpr long long kDblMinBits = 0x0010000000000000LL;  // bits of DBL_MIN
 
-// One state per block of LU_WARPS warps, its matrix in shared memory (odd
-// row pitch: a column read by 32 lanes is free of bank conflicts).  Step k:
-// every warp finds the pivot (integer comparison of |a| bit patterns, no
-// FP64 instruction); warp 0 forms the interchanged multiplier column scaled
-// by the reciprocal into lvec while all threads interchange the other
-// columns of rows k and p; after a barrier the trailing block gets the rank-1
-// update (elements spread flat over the block's threads, LU_BATCH per thread at
-// a time) and column k takes lvec; a second barrier closes the step.
-#ifndef LU_WARPS
-#define LU_WARPS 2  // 193 ms per 1M GRI states; 1, 3 and 4 warps: 201, 211, 205 ms
+// S consecutive states per block (4, or 2 or 1 where four matrices do not fit
+// in shared memory) of 32 S threads, each matrix in shared memory with an odd
+// row pitch (a column read by 32 lanes is free of bank conflicts).  Step k:
+// warp w alone works on state w - the pivot (first largest |a|, compared as
+// integer bit patterns, no FP64 instruction), the multiplier column scaled by
+// the reciprocal (read through the interchange) and the interchange of the
+// other columns of rows k and p; after a barrier every thread updates one
+// trailing position in all S states (rows are interchanged in place, so the
+// positions agree across states); a second barrier closes the step.  Loads
+// and stores give each thread one state, so F-order accesses cover whole
+// 32-byte sectors.
+constexpr int kLuMaxStates = 4;
+#ifndef PJG_LU_WPS
+#define PJG_LU_WPS 2
 #endif
-#ifndef LU_MINB
-#define LU_MINB 9
-#endif
-#ifndef LU_BATCH
-#define LU_BATCH 4  // trailing elements a thread loads before it stores
-#endif
-#define LU_THREADS (32 * LU_WARPS)
+constexpr int kWarpsPerState = PJG_LU_WPS;  // threads per block = 32 * S * kWarpsPerState
 
-template <bool F>
-__global__ void __launch_bounds__(LU_THREADS, LU_MINB) lu_factor_kernel(int nn, long long n, double s,
-                                                                  const double* __restrict__ h,
-                                                                  double h0, const double* jac,
-                                                                  double* lu,
-                                                                  int32_t* __restrict__ piv,
-                                                                  int32_t* __restrict__ info)
+template <bool F, int S>
+__global__ void __launch_bounds__(32 * S * kWarpsPerState) lu_factor_kernel(int nn, long long n, double s,
+                                                           const double* __restrict__ h, double h0,
+                                                           const double* jac, double* lu,
+                                                           int32_t* __restrict__ piv,
+                                                           int32_t* __restrict__ info)
 {
     extern __shared__ double smem[];
+    __shared__ double gst[S];
+    constexpr int T = 32 * S * kWarpsPerState, TS = T / S;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int pitch = nn | 1;
-    double* a = smem;
-    double* lvec = a + (size_t)nn * pitch;
-    int* sp = reinterpret_cast<int*>(lvec + nn);
+    const int msz = nn * pitch;
     const int nsq = nn * nn;
-    for (long long i = blockIdx.x; i < n; i += gridDim.x) {
-        const double g = s * (h ? h[i] : h0);
+    int* sp_base = reinterpret_cast<int*>(smem + (size_t)S * msz);
+    const int ws = warp < S ? warp : 0;
+    double* Aw = smem + (size_t)ws * msz;  // the pivot phase: warp w < S, state w
+    int* spw = sp_base + ws * nn;
+    const int my = tid % S, lane_s = tid / S;  // loads and stores: one state per thread
+    double* Am = smem + (size_t)my * msz;
+    const long long ngroups = (n + S - 1) / S;
+    for (long long grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        const long long i0 = grp * S;
+        const int here = (int)((n - i0) < S ? (n - i0) : S);
+        if (tid < S) gst[tid] = tid < here ? s * (h ? h[i0 + tid] : h0) : 0.0;
+        __syncthreads();
         {
-            Cursor cu(tid, LU_THREADS, nn);
-            for (int e = tid; e < nsq; e += LU_THREADS) {
-                const double j = jac[mat_idx(F, i, n, nn, cu.r, cu.c)];
-                a[cu.r * pitch + cu.c] = fma(-g, j, cu.r == cu.c ? 1.0 : 0.0);
+            const double g = gst[my];
+            const bool live = my < here;
+            Cursor cu(lane_s, TS, nn);
+            for (int e = lane_s; e < nsq; e += TS) {
+                const double j = live ? jac[mat_idx(F, i0 + my, n, nn, cu.r, cu.c)] : 0.0;
+                Am[cu.r * pitch + cu.c] = fma(-g, j, cu.r == cu.c ? 1.0 : 0.0);
                 cu.next();
             }
         }
         __syncthreads();
-        int first_zero = 0;  // thread 0's
+        int first_zero = 0;  // lane 0 of warp w, for state w
         for (int k = 0; k < nn; ++k) {
-            long long best = -1;
-            int br = k;
-            for (int r = k + lane; r < nn; r += 32) {
-                const long long v = __double_as_longlong(a[r * pitch + k]) & kAbsMask;
-                if (v > best) {
-                    best = v;
-                    br = r;
+            if (warp < S) {
+                long long best = -1;
+                int br = k;
+                for (int r = k + lane; r < nn; r += 32) {
+                    const long long v = __double_as_longlong(Aw[r * pitch + k]) & kAbsMask;
+                    if (v > best) {
+                        best = v;
+                        br = r;
+                    }
                 }
-            }
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
-                const int orr = __shfl_xor_sync(0xffffffffu, br, off);
-                if (ob > best || (ob == best && orr < br)) {
-                    best = ob;
-                    br = orr;
+                for (int off = 16; off > 0; off >>= 1) {
+                    const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+                    const int orr = __shfl_xor_sync(0xffffffffu, br, off);
+                    if (ob > best || (ob == best && orr < br)) {
+                        best = ob;
+                        br = orr;
+                    }
                 }
-            }
-            const bool nonzero = best != 0;
-            const int m = nn - k - 1;
-            double p = 0.0;
-            if (warp == 0) {
-                p = a[br * pitch + k];
+                const bool nonzero = best != 0;
+                const double p = Aw[br * pitch + k];
+                __syncwarp();  // every lane has read the pivot before row br's lane rewrites it
                 if (lane == 0) {
-                    sp[k] = br + 1;
+                    spw[k] = br + 1;
                     if (!nonzero && !first_zero) first_zero = k + 1;
                 }
                 const bool recip = best >= kDblMinBits;
                 const double inv = (nonzero && recip) ? __drcp_rn(p) : 0.0;
+                // multipliers of rows r > k, read through the interchange; a lane
+                // reads its own rows and row k, and writes only its own rows
                 for (int r = k + 1 + lane; r < nn; r += 32) {
-                    double v = a[(r == br ? k : r) * pitch + k];
+                    double v = Aw[(r == br ? k : r) * pitch + k];
                     if (nonzero) v = recip ? v * inv : v / p;
-                    lvec[r] = v;
+                    Aw[r * pitch + k] = v;
                 }
+                if (nonzero && br != k)
+                    for (int c = lane; c < nn; c += 32)
+                        if (c != k) {
+                            const double t = Aw[k * pitch + c];
+                            Aw[k * pitch + c] = Aw[br * pitch + c];
+                            Aw[br * pitch + c] = t;
+                        }
+                __syncwarp();
+                if (lane == 0 && nonzero) Aw[k * pitch + k] = p;
             }
-            if (nonzero && br != k)
-                for (int c = tid; c < nn; c += LU_THREADS)
-                    if (c != k) {
-                        const double t = a[k * pitch + c];
-                        a[k * pitch + c] = a[br * pitch + c];
-                        a[br * pitch + c] = t;
-                    }
             __syncthreads();
-            if (tid == 0 && nonzero) a[k * pitch + k] = p;
-            for (int r = k + 1 + tid; r < nn; r += LU_THREADS) a[r * pitch + k] = lvec[r];
+            const int m = nn - k - 1;
             const int mm = m * m;
             if (tid < mm) {
-                const double* urow = a + k * pitch + k + 1;
-                const double* lv = lvec + k + 1;
-                double* t = a + (k + 1) * pitch + k + 1;
-                Cursor cu(tid, LU_THREADS, m);
-                for (int e = tid; e < mm; e += LU_BATCH * LU_THREADS) {
-                    int o[LU_BATCH];
-                    double l[LU_BATCH], u[LU_BATCH], v[LU_BATCH];
-                    bool ok[LU_BATCH];
+                const int base = (k + 1) * pitch + k + 1;
+                Cursor cu(tid, T, m);
+                for (int e = tid; e < mm; e += T) {
+                    const int o = base + cu.r * pitch + cu.c;
+                    const int ol = (k + 1 + cu.r) * pitch + k, ou = k * pitch + k + 1 + cu.c;
+                    double l[S], u[S], v[S];
 #pragma unroll
-                    for (int q = 0; q < LU_BATCH; ++q) {
-                        ok[q] = e + q * LU_THREADS < mm;
-                        o[q] = cu.r * pitch + cu.c;
-                        if (ok[q]) {
-                            l[q] = lv[cu.r];
-                            u[q] = urow[cu.c];
-                            v[q] = t[o[q]];
-                        }
-                        cu.next();
+                    for (int q = 0; q < S; ++q) {
+                        const double* B = smem + (size_t)q * msz;
+                        l[q] = B[ol];
+                        u[q] = B[ou];
+                        v[q] = B[o];
                     }
 #pragma unroll
-                    for (int q = 0; q < LU_BATCH; ++q)
-                        if (ok[q]) t[o[q]] = fma(-l[q], u[q], v[q]);
+                    for (int q = 0; q < S; ++q) smem[(size_t)q * msz + o] = fma(-l[q], u[q], v[q]);
+                    cu.next();
                 }
             }
             __syncthreads();
         }
-        {
-            Cursor cu(tid, LU_THREADS, nn);
-            for (int e = tid; e < nsq; e += LU_THREADS) {
-                lu[mat_idx(F, i, n, nn, cu.r, cu.c)] = a[cu.r * pitch + cu.c];
+        if (my < here) {
+            Cursor cu(lane_s, TS, nn);
+            for (int e = lane_s; e < nsq; e += TS) {
+                lu[mat_idx(F, i0 + my, n, nn, cu.r, cu.c)] = Am[cu.r * pitch + cu.c];
                 cu.next();
             }
+            const int* spm = sp_base + my * nn;
+            for (int k = lane_s; k < nn; k += TS) piv[vec_idx(F, i0 + my, n, nn, k)] = spm[k];
         }
-        for (int k = tid; k < nn; k += LU_THREADS) piv[vec_idx(F, i, n, nn, k)] = sp[k];
-        if (tid == 0 && info) info[i] = first_zero;
+        if (lane == 0 && warp < S && warp < here && info) info[i0 + warp] = first_zero;
         __syncthreads();
     }
 }
@@ -214,9 +220,13 @@ __global__ void __launch_bounds__(LU_THREADS, LU_MINB) lu_factor_kernel(int nn, 
 // index lists ridx (R_k), cidx (C_k), lidx (columns c < r of L's row r),
 // uidx (columns c > r of U's row r).
 struct LuPlanView {
-    int nn;
+    int nn, nR, nC;  // nR = roff[nn], nC = coff[nn]
     const int *perm, *roff, *coff, *loff, *uoff, *ridx, *cidx, *lidx, *uidx;
 };
+
+// ints of the plan the factorisation reads: roff, coff [nn + 1], perm [nn],
+// ridx [nR], cidx [nC]
+inline int plan_factor_ints(const LuPlanView& v) { return 3 * v.nn + 2 + v.nR + v.nC; }
 
 // S consecutive states per block (4, or 2 or 1 where four matrices do not fit
 // in shared memory), eliminated in lockstep by 32 S threads: in loads,
@@ -225,16 +235,18 @@ struct LuPlanView {
 // for all S states, so one index lookup and one barrier pair serve S states.
 constexpr int kLusMaxStates = 4;
 
-template <bool F, int S>
-__global__ void __launch_bounds__(32 * S) lu_sparse_kernel(long long n, double s,
-                                                           const double* __restrict__ h, double h0,
-                                                           const double* jac, double* lu,
-                                                           int32_t* __restrict__ info, LuPlanView pl)
+template <bool F, int S, bool TSM>
+__global__ void __launch_bounds__(32 * S * kWarpsPerState) lu_sparse_kernel(long long n, double s,
+                                                                            const double* __restrict__ h,
+                                                                            double h0, const double* jac,
+                                                                            double* lu,
+                                                                            int32_t* __restrict__ info,
+                                                                            LuPlanView pl)
 {
     extern __shared__ double smem[];
     __shared__ double gst[S];
     __shared__ int fz[S];
-    constexpr int T = 32 * S, TS = 32;
+    constexpr int T = 32 * S * kWarpsPerState, TS = T / S;
     const int nn = pl.nn;
     const int tid = threadIdx.x;
     const int pitch = nn | 1;
@@ -243,6 +255,24 @@ __global__ void __launch_bounds__(32 * S) lu_sparse_kernel(long long n, double s
     const int my = tid % S;   // this thread's state slot in loads, stores and scalings
     const int lane_s = tid / S;
     double* A = smem + (size_t)my * msz;
+    // the plan's index lists, in shared memory when they fit beside the matrices
+    const int *proff = pl.roff, *pcoff = pl.coff, *pperm = pl.perm, *pridx = pl.ridx, *pcidx = pl.cidx;
+    if (TSM) {
+        int* tb = reinterpret_cast<int*>(smem + (size_t)S * msz);
+        for (int q = tid; q <= nn; q += T) {
+            tb[q] = pl.roff[q];
+            tb[nn + 1 + q] = pl.coff[q];
+        }
+        for (int q = tid; q < nn; q += T) tb[2 * nn + 2 + q] = pl.perm[q];
+        for (int q = tid; q < pl.nR; q += T) tb[3 * nn + 2 + q] = pl.ridx[q];
+        for (int q = tid; q < pl.nC; q += T) tb[3 * nn + 2 + pl.nR + q] = pl.cidx[q];
+        proff = tb;
+        pcoff = tb + nn + 1;
+        pperm = tb + 2 * nn + 2;
+        pridx = tb + 3 * nn + 2;
+        pcidx = pridx + pl.nR;
+        __syncthreads();
+    }
     const long long ngroups = (n + S - 1) / S;
     for (long long grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const long long i0 = grp * S;
@@ -257,28 +287,26 @@ __global__ void __launch_bounds__(32 * S) lu_sparse_kernel(long long n, double s
             const bool live = my < here;
             Cursor cu(lane_s, TS, nn);
             for (int e = lane_s; e < nsq; e += TS) {
-                const double j = live ? jac[mat_idx(F, i0 + my, n, nn, __ldg(pl.perm + cu.r),
-                                                    __ldg(pl.perm + cu.c))]
-                                      : 0.0;
+                const double j = live ? jac[mat_idx(F, i0 + my, n, nn, pperm[cu.r], pperm[cu.c])] : 0.0;
                 A[cu.r * pitch + cu.c] = fma(-g, j, cu.r == cu.c ? 1.0 : 0.0);
                 cu.next();
             }
         }
         __syncthreads();
         for (int k = 0; k < nn; ++k) {
-            const int r0 = __ldg(pl.roff + k), nr = __ldg(pl.roff + k + 1) - r0;
+            const int r0 = proff[k], nr = proff[k + 1] - r0;
             if (tid < S && smem[(size_t)tid * msz + k * pitch + k] == 0.0 && !fz[tid]) fz[tid] = k + 1;
             if (nr == 0) continue;  // nothing below the pivot: no update, no barrier
-            const int c0 = __ldg(pl.coff + k), nc = __ldg(pl.coff + k + 1) - c0;
-            const int* R = pl.ridx + r0;
-            const int* C = pl.cidx + c0;
+            const int c0 = pcoff[k], nc = pcoff[k + 1] - c0;
+            const int* R = pridx + r0;
+            const int* C = pcidx + c0;
             if (lane_s < nr) {
                 const double p = A[k * pitch + k];
                 if (p != 0.0) {
                     const bool recip = fabs(p) >= DBL_MIN;
                     const double inv = recip ? __drcp_rn(p) : 0.0;
                     for (int q = lane_s; q < nr; q += TS) {
-                        double* x = A + __ldg(R + q) * pitch + k;
+                        double* x = A + R[q] * pitch + k;
                         *x = recip ? *x * inv : *x / p;
                     }
                 }
@@ -288,7 +316,7 @@ __global__ void __launch_bounds__(32 * S) lu_sparse_kernel(long long n, double s
             if (tid < mm) {
                 Cursor cu(tid, T, nc);
                 for (int e = tid; e < mm; e += T) {
-                    const int r = __ldg(R + cu.r), c = __ldg(C + cu.c);
+                    const int r = R[cu.r], c = C[cu.c];
                     const int o = r * pitch + c, ol = r * pitch + k, ou = k * pitch + c;
                     double l[S], u[S], v[S];
 #pragma unroll
@@ -409,29 +437,44 @@ __global__ void ros2_combine_kernel(int op, int nn, long long n, const double* _
     }
 }
 
-int lu_factor_config(int nn, size_t* smem, int* grid)
+template <int S>
+int lu_factor_launch(int nn, long long n, char order, double s, const double* h, double h0,
+                     const double* jac, double* lu, int32_t* piv, int32_t* info, cudaStream_t st, int sms)
 {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            return pjg_internal_fail(PJG_ERR_CUDA, "device query failed");
-    }
-    *smem = (size_t)nn * (nn | 1) * sizeof(double) + (size_t)nn * (sizeof(double) + sizeof(int));
-    const void* fn = (const void*)lu_factor_kernel<false>;
-    const void* fnF = (const void*)lu_factor_kernel<true>;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess ||
-        cudaFuncSetAttribute(fnF, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem) != cudaSuccess)
+    const size_t smem = (size_t)S * ((size_t)nn * (nn | 1) * sizeof(double) + (size_t)nn * sizeof(int));
+    const void* fn = (const void*)lu_factor_kernel<false, S>;
+    const void* fnF = (const void*)lu_factor_kernel<true, S>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(fnF, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return pjg_internal_fail(PJG_ERR_CUDA, "cannot reserve shared memory for the LU kernel");
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, LU_THREADS, *smem) != cudaSuccess ||
-        per_sm < 1)
+    const int threads = 32 * S * kWarpsPerState;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess || per_sm < 1)
         return pjg_internal_fail(PJG_ERR_CUDA, "LU kernel does not fit on the device");
-    *grid = sms * per_sm;
+    long long grid = (long long)sms * per_sm;
+    const long long groups = (n + S - 1) / S;
+    if (groups < grid) grid = groups;
+    if (order == 'F')
+        lu_factor_kernel<true, S><<<(int)grid, threads, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
+    else
+        lu_factor_kernel<false, S><<<(int)grid, threads, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
     return 0;
 }
 
+int sm_count(int* sms)
+{
+    static int cached = 0;
+    if (!cached) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return pjg_internal_fail(PJG_ERR_CUDA, "device query failed");
+    }
+    *sms = cached;
+    return 0;
+}
+
+constexpr size_t kSmemLimit = (227u << 10) - 64;  // opt-in shared memory of one block, less the static part
 
 // ---- host side of the static-pivot plan
 
@@ -530,26 +573,28 @@ static int build_plan_tables(int nn, const int* row_ptr, const int* col_ind, std
     return 0;
 }
 
-template <int S>
+template <int S, bool TSM>
 int lu_sparse_launch(const LuPlan* pl, long long n, char order, double s, const double* h, double h0,
                      const double* jac, double* lu, int32_t* info, cudaStream_t st, int sms)
 {
-    const size_t smem = (size_t)S * pl->nn * (pl->nn | 1) * sizeof(double);
-    const void* fn = (const void*)lu_sparse_kernel<false, S>;
-    const void* fnF = (const void*)lu_sparse_kernel<true, S>;
+    const size_t smem = (size_t)S * pl->nn * (pl->nn | 1) * sizeof(double) +
+                        (TSM ? (size_t)plan_factor_ints(pl->view) * sizeof(int) : 0);
+    const void* fn = (const void*)lu_sparse_kernel<false, S, TSM>;
+    const void* fnF = (const void*)lu_sparse_kernel<true, S, TSM>;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
         cudaFuncSetAttribute(fnF, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return pjg_internal_fail(PJG_ERR_CUDA, "cannot reserve shared memory for the sparse LU kernel");
+    const int threads = 32 * S * kWarpsPerState;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * S, smem) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess || per_sm < 1)
         return pjg_internal_fail(PJG_ERR_CUDA, "sparse LU kernel does not fit on the device");
     long long grid = (long long)sms * per_sm;
     const long long groups = (n + S - 1) / S;
     if (groups < grid) grid = groups;
     if (order == 'F')
-        lu_sparse_kernel<true, S><<<(int)grid, 32 * S, smem, st>>>(n, s, h, h0, jac, lu, info, pl->view);
+        lu_sparse_kernel<true, S, TSM><<<(int)grid, threads, smem, st>>>(n, s, h, h0, jac, lu, info, pl->view);
     else
-        lu_sparse_kernel<false, S><<<(int)grid, 32 * S, smem, st>>>(n, s, h, h0, jac, lu, info, pl->view);
+        lu_sparse_kernel<false, S, TSM><<<(int)grid, threads, smem, st>>>(n, s, h, h0, jac, lu, info, pl->view);
     return 0;
 }
 
@@ -564,14 +609,17 @@ extern "C" int pjg_internal_lu_factor(int32_t nn, int64_t n, char order, double 
     if (order != 'C' && order != 'F') return pjg_internal_fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
     if (n == 0) return 0;
     if (!jac || !lu || !piv) return pjg_internal_fail(PJG_ERR_ARG, "null array");
-    int grid = 1;
-    size_t smem = 0;
-    if (int rc = lu_factor_config(nn, &smem, &grid)) return rc;
-    if (n < grid) grid = (int)n;
-    if (order == 'F')
-        lu_factor_kernel<true><<<grid, LU_THREADS, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
+    int sms = 0;
+    if (int rc = sm_count(&sms)) return rc;
+    const size_t per_state = (size_t)nn * (nn | 1) * sizeof(double) + (size_t)nn * sizeof(int);
+    int rc;
+    if (kLuMaxStates * per_state <= kSmemLimit)
+        rc = lu_factor_launch<kLuMaxStates>(nn, n, order, s, h, h0, jac, lu, piv, info, st, sms);
+    else if (2 * per_state <= kSmemLimit)
+        rc = lu_factor_launch<2>(nn, n, order, s, h, h0, jac, lu, piv, info, st, sms);
     else
-        lu_factor_kernel<false><<<grid, LU_THREADS, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
+        rc = lu_factor_launch<1>(nn, n, order, s, h, h0, jac, lu, piv, info, st, sms);
+    if (rc) return rc;
     pjg_internal_count_launch();
     if (cudaGetLastError() != cudaSuccess) return pjg_internal_fail(PJG_ERR_CUDA, "LU factor launch failed");
     return 0;
@@ -638,6 +686,8 @@ extern "C" int pjg_internal_lu_plan_create(int32_t nn, const int32_t* row_ptr, c
     v.loff = v.coff + nn + 1;
     v.uoff = v.loff + nn + 1;
     v.ridx = v.uoff + nn + 1;
+    v.nR = tab[2 * nn];
+    v.nC = tab[3 * nn + 1];
     v.cidx = v.ridx + tab[2 * nn];      // + roff[nn]
     v.lidx = v.cidx + tab[3 * nn + 1];  // + coff[nn]
     v.uidx = v.lidx + tab[4 * nn + 2];  // + loff[nn]
@@ -671,22 +721,26 @@ extern "C" int pjg_internal_lu_factor_sparse(const void* p, int64_t n, char orde
     if (order != 'C' && order != 'F') return pjg_internal_fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
     if (n == 0) return 0;
     if (!jac || !lu) return pjg_internal_fail(PJG_ERR_ARG, "null array");
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            return pjg_internal_fail(PJG_ERR_CUDA, "device query failed");
-    }
+    int sms = 0;
+    if (int rc = sm_count(&sms)) return rc;
+    // states per block: the most (4, 2, 1) whose matrices fit, with the
+    // plan's index lists beside them when those fit too
     const size_t per_state = (size_t)pl->nn * (pl->nn | 1) * sizeof(double);
-    const size_t limit = (227u << 10) - 64;  // opt-in shared memory of one block, less the static part
+    const size_t tabs = (size_t)plan_factor_ints(pl->view) * sizeof(int);
+    const size_t limit = kSmemLimit;
     int rc;
-    if (kLusMaxStates * per_state <= limit)
-        rc = lu_sparse_launch<kLusMaxStates>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
+    if (kLusMaxStates * per_state + tabs <= limit)
+        rc = lu_sparse_launch<kLusMaxStates, true>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
+    else if (kLusMaxStates * per_state <= limit)
+        rc = lu_sparse_launch<kLusMaxStates, false>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
+    else if (2 * per_state + tabs <= limit)
+        rc = lu_sparse_launch<2, true>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
     else if (2 * per_state <= limit)
-        rc = lu_sparse_launch<2>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
+        rc = lu_sparse_launch<2, false>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
+    else if (per_state + tabs <= limit)
+        rc = lu_sparse_launch<1, true>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
     else
-        rc = lu_sparse_launch<1>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
+        rc = lu_sparse_launch<1, false>(pl, n, order, s, h, h0, jac, lu, info, st, sms);
     if (rc) return rc;
     pjg_internal_count_launch();
     if (cudaGetLastError() != cudaSuccess) return pjg_internal_fail(PJG_ERR_CUDA, "sparse LU launch failed");
