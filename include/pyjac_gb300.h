@@ -102,6 +102,13 @@ int pjg_species_rates(pjg_mech* mech, int64_t n, char order, int conp, const dou
                       const double* phi, double* dphi, void* stream);
 int pjg_jacobian(pjg_mech* mech, int64_t n, char order, int conp, int jac_format,
                  const double* param, const double* phi, double* jac, void* stream);
+/* The Jacobian and the species rates of the same states in one pass (an
+ * implicit solver needs both at every step): jac as pjg_jacobian writes it,
+ * dphi (laid out like phi) bit for bit as pjg_species_rates writes it.  No
+ * reference counterpart (the reference evaluates them in separate kernels). */
+int pjg_jacobian_rates(pjg_mech* mech, int64_t n, char order, int conp, int jac_format,
+                       const double* param, const double* phi, double* jac, double* dphi,
+                       void* stream);
 /* Species thermo, the chem_utils kernel type (pyjac/core/rate_subs.py
  * write_chem_utils :3391-3444; examples/opencl/ch4/chem_utils.ocl:49): at
  * the guarded temperature T = min(max(phi_T, 100 K), 10,000 K) of each state,
@@ -239,9 +246,10 @@ int pjg_write_initial_conditions(const char* filename, int64_t n, int32_t nn, ch
  * pjg_lu_solve_sparse: b (laid out like phi, variables' order) <- M^-1 b.
  *
  * pjg_ros2_step: one step of the L-stable Rosenbrock method ROS2
- * (gamma = 1 + 1/sqrt 2) from phi with step h_i: rates and dense Jacobian at
- * phi, one factorisation (lu_kind 0: partial pivoting; 1: the static-pivot
- * sparse plan), two solves, one more rates evaluation;
+ * (gamma = 1 + 1/sqrt 2) from phi with step h_i: dense Jacobian and rates
+ * at phi in one pass (pjg_jacobian_rates), one factorisation (lu_kind 0:
+ * partial pivoting; 1: the static-pivot sparse plan), two solves, one more
+ * rates evaluation;
  * phi_new = phi + 1.5 h k1 + 0.5 h k2 and, if err is not NULL, the embedded
  * first-order error estimate err = 0.5 h (k1 + k2).  Work arrays: jac_work
  * n*nn*nn doubles (holds the factors on return), piv_work n*nn int32

@@ -32,6 +32,8 @@ SIGNATURES = [
      [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, _VP, _VP, _VP, _VP]),
     ("pjg_jacobian", ctypes.c_int,
      [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP]),
+    ("pjg_jacobian_rates", ctypes.c_int,
+     [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP, _VP]),
     ("pjg_vjp", ctypes.c_int,
      [_VP, ctypes.c_int64, ctypes.c_char, ctypes.c_int, _VP, _VP, _VP, _VP, _VP]),
     ("pjg_vjp_noalloc", ctypes.c_int,

@@ -145,7 +145,9 @@ class Evaluator(DeviceMechanism):
             out.data_ptr(), st))
         return out
 
-    def jacobian(self, param, phi, order="C", conp=True, jac_format="full", out=None):
+    def jacobian(self, param, phi, order="C", conp=True, jac_format="full", out=None, dphi=None):
+        """The Jacobian; with ``dphi`` (a tensor like phi) the species rates of
+        the same pass are written there too (pjg_jacobian_rates)."""
         import torch
         n, st = self._prep(param, phi, order)
         fmt = _fmt(jac_format)
@@ -158,6 +160,13 @@ class Evaluator(DeviceMechanism):
             out = torch.empty(shape, dtype=torch.float64, device=phi.device)
         elif out.numel() != n * per:
             raise ValueError("output must hold %d values" % (n * per))
+        if dphi is not None:
+            if dphi.shape != phi.shape or dphi.dtype != torch.float64 or not dphi.is_contiguous():
+                raise ValueError("dphi must match phi")
+            _lib.check("pjg_jacobian_rates", self._lib.pjg_jacobian_rates(
+                self.handle, n, _order(order), int(bool(conp)), fmt, param.data_ptr(),
+                phi.data_ptr(), out.data_ptr(), dphi.data_ptr(), st))
+            return out
         _lib.check("pjg_jacobian", self._lib.pjg_jacobian(
             self.handle, n, _order(order), int(bool(conp)), fmt, param.data_ptr(), phi.data_ptr(),
             out.data_ptr(), st))

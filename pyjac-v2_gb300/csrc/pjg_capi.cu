@@ -302,9 +302,12 @@ size_t eval_state_bytes(const pjg_mech* m, int kind, bool F, const SlotTables* t
 // Evaluate n states.  The per-state working arrays go to ext_work (ext_bytes)
 // when given, else to the mechanism's shared buffer, grown on demand; larger
 // problems run as several launches.
+// For the Jacobian, dphi (optional, laid out like phi) also receives the
+// species rates of the same pass.
 int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_format,
              const double* param, const double* phi, double* out, cudaStream_t st,
-             const double* v = nullptr, double* ext_work = nullptr, size_t ext_bytes = 0)
+             const double* v = nullptr, double* ext_work = nullptr, size_t ext_bytes = 0,
+             double* dphi = nullptr)
 {
     if (!m) return fail(PJG_ERR_ARG, "null mechanism");
     if (n < 0) return fail(PJG_ERR_ARG, "negative problem size");
@@ -362,6 +365,11 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
             a.v = F ? v + off : v + off * NN;
             a.vjp = F ? out + off : out + off * NN;
         } else {
+            if (dphi) {
+                a.dphi = F ? dphi + off : dphi + off * NN;
+                a.dphi_ss = a.phi_ss;
+                a.dphi_sj = a.phi_sj;
+            }
             a.nslot = t->nslot;
             if (F) {
                 a.acc = out + off;
@@ -720,6 +728,14 @@ int pjg_jacobian(pjg_mech* m, int64_t n, char order, int conp, int jac_format, c
                     (cudaStream_t)stream);
 }
 
+int pjg_jacobian_rates(pjg_mech* m, int64_t n, char order, int conp, int jac_format,
+                       const double* param, const double* phi, double* jac, double* dphi, void* stream)
+{
+    if (n > 0 && !dphi) return fail(PJG_ERR_ARG, "null array");
+    return run_eval(m, PJG_JACOBIAN, n, order, conp, jac_format, param, phi, jac, (cudaStream_t)stream,
+                    nullptr, nullptr, 0, dphi);
+}
+
 int pjg_vjp(pjg_mech* m, int64_t n, char order, int conp, const double* param, const double* phi,
             const double* v, double* out, void* stream)
 {
@@ -776,7 +792,8 @@ int pjg_lu_solve_sparse(pjg_mech* m, int64_t n, char order, const double* lu, do
 // 20(4), 1999), gamma = 1 + 1/sqrt(2):
 //   (I - gamma h J) k1 = f(y),  (I - gamma h J) k2 = f(y + h k1) - 2 k1,
 //   y_new = y + 1.5 h k1 + 0.5 h k2,  err = y_new - (y + h k1) = 0.5 h (k1 + k2),
-// with J the analytical Jacobian at y and f the species rates.  lu_kind 0
+// with J the analytical Jacobian at y and f the species rates (f(y) from the
+// Jacobian's own pass, so one rates evaluation per step).  lu_kind 0
 // factors with partial pivoting, 1 with the mechanism's static-pivot sparse
 // plan (piv_work unused).
 int pjg_ros2_step(pjg_mech* m, int64_t n, char order, int conp, const double* param,
@@ -808,8 +825,9 @@ int pjg_ros2_step(pjg_mech* m, int64_t n, char order, int conp, const double* pa
     };
     double* k1 = vec_work;
     double* k2 = vec_work + (size_t)n * nn;
-    int rc = run_eval(m, PJG_SPECIES_RATES, n, order, conp, 0, param, phi, k1, st);
-    if (!rc) rc = run_eval(m, PJG_JACOBIAN, n, order, conp, PJG_JAC_FULL, param, phi, jac_work, st);
+    // f(y) comes out of the Jacobian's pass
+    int rc = run_eval(m, PJG_JACOBIAN, n, order, conp, PJG_JAC_FULL, param, phi, jac_work, st, nullptr,
+                      nullptr, 0, k1);
     if (!rc) rc = factor();
     if (!rc) rc = solve(k1);
     if (!rc) rc = pjg_internal_ros2_combine(0, nn, n, order, h, h0, phi, k1, nullptr, phi_new, nullptr, st);

@@ -312,3 +312,23 @@ def test_lu_factor_sparse_large_mechanisms(cuda_device, tmp_path, n_species, sta
     lu_p, piv_p, _ = orc.lu_factor(J, integ.ROS2_GAMMA, 1e-2)
     assert np.array_equal(bits(lu_d.cpu().numpy()), bits(lu_p))
     assert np.array_equal(piv_d.cpu().numpy(), piv_p)
+
+
+@pytest.mark.parametrize("order", ["C", "F"])
+@pytest.mark.parametrize("fmt", ["full", "sparse"])
+@pytest.mark.parametrize("name", ["h2o2", "gri30"])
+def test_jacobian_rates_one_pass_bitwise(cuda_device, order, fmt, name):
+    """pjg_jacobian_rates: the Jacobian equals pjg_jacobian's and the rates
+    equal pjg_species_rates', bit for bit, from one pass."""
+    import torch
+    mech = load_mech(name)
+    n = 1000
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=27, x_floor=1e-12)
+    ev = pkg("api").Evaluator(mech)
+    Pd, phid = torch.from_numpy(P).to(cuda_device), _to_dev_vec(phi, order, cuda_device)
+    dphi = torch.empty_like(phid)
+    J1 = ev.jacobian(Pd, phid, order=order, jac_format=fmt, dphi=dphi)
+    J0 = ev.jacobian(Pd, phid, order=order, jac_format=fmt)
+    r0 = ev.species_rates(Pd, phid, order=order)
+    assert torch.equal(J1, J0)
+    assert torch.equal(dphi, r0)
