@@ -174,7 +174,8 @@ class Ros2Stepper(object):
         n = max(self.capacity, 1)
         self.lu = torch.empty((n, nn, nn) if order == "C" else (nn, nn, n), dtype=torch.float64,
                               device=dev)
-        self.piv = torch.empty((n, nn) if order == "C" else (nn, n), dtype=torch.int32, device=dev)
+        self.piv = (torch.empty((n, nn) if order == "C" else (nn, n), dtype=torch.int32, device=dev)
+                    if lu_kind == "pivoting" else None)
         self.vec = torch.empty(2 * n * nn, dtype=torch.float64, device=dev)
         self.info = torch.empty(n, dtype=torch.int32, device=dev)
 
@@ -191,6 +192,6 @@ class Ros2Stepper(object):
         _lib.check("pjg_ros2_step", self.ev._lib.pjg_ros2_step(
             self.ev.handle, n, _order(self.order), int(bool(conp)), param.data_ptr(), phi.data_ptr(),
             hp, h0, 0 if self.lu_kind == "pivoting" else 1, out.data_ptr(), err.data_ptr(),
-            self.lu.data_ptr(), self.piv.data_ptr(),
+            self.lu.data_ptr(), None if self.piv is None else self.piv.data_ptr(),
             self.vec.data_ptr(), self.info.data_ptr(), st))
         return out, err, self.info[:n]
