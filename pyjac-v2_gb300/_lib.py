@@ -61,6 +61,8 @@ SIGNATURES = [
     ("pjg_mlp_forward", ctypes.c_int,
      [_VP, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(_VP), ctypes.POINTER(_VP), _VP,
       ctypes.c_int64, _VP]),
+    ("pjg_host_register", ctypes.c_int, [_VP, ctypes.c_size_t]),
+    ("pjg_host_unregister", ctypes.c_int, [_VP]),
     ("pjg_launch_count", ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
     ("pjg_fp64_peak", ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     ("pjg_profile_begin", ctypes.c_int, []),

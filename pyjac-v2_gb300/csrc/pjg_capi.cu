@@ -564,6 +564,20 @@ int pjg_math_exp(const double* x, double* y, int64_t n, void* stream)
     return 0;
 }
 
+int pjg_host_register(void* ptr, size_t bytes)
+{
+    if (!ptr || !bytes) return fail(PJG_ERR_ARG, "null or empty host range");
+    CUDA_TRY(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+    return 0;
+}
+
+int pjg_host_unregister(void* ptr)
+{
+    if (!ptr) return fail(PJG_ERR_ARG, "null host pointer");
+    CUDA_TRY(cudaHostUnregister(ptr));
+    return 0;
+}
+
 int pjg_launch_count(int64_t* count)
 {
     if (!count) return fail(PJG_ERR_ARG, "null argument");

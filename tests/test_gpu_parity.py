@@ -313,3 +313,30 @@ def test_approximate_jacobian(cuda_device, name, order, fmt):
                       jac_format=fmt).cpu().numpy()
     assert np.isfinite(out).all()
     assert row_rel_err(_dense_from(out, order, fmt, mech, ev, n), Jref) < RTOL_JAC
+
+
+def test_pywrap_kernel_registered_host_arrays(cuda_device):
+    """The kernel object into host arrays page-locked in place
+    (hostmem.empty -> pjg_host_register) gives the same Jacobian as into
+    pageable arrays; the registration is released with the array."""
+    import gc
+    mech = load_mech("gri30")
+    n = 20000
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=44, x_floor=1e-12)
+    x = np.ascontiguousarray(phi.T)
+    hm = pkg("hostmem")
+    mod = pkg("api").pywrap(mech, order="F")
+    k = mod.PyJacobianKernel(n, 1)
+    ref = np.empty(n * mech.nn * mech.nn)
+    k(P, x, ref)
+    hP = hm.empty(P.shape)
+    hx = hm.empty(x.shape)
+    hout = hm.empty(ref.shape)
+    hP[:] = P
+    hx[:] = x
+    k(hP, hx, hout)
+    assert np.array_equal(hout, ref)
+    k.close()
+    del hP, hx, hout
+    gc.collect()
+    assert not pkg("hostmem")._keep
