@@ -13,10 +13,10 @@
 // pivots as vectors of int32 (1-based, LAPACK's ipiv).
 //
 // FP64 on GB300 issues one warp instruction per 16 clocks per SM whatever the
-// number of active lanes, so the factorisation spreads each state's flattened
-// trailing block over the threads of a block (one state per block, its matrix
-// in shared memory) to keep the lanes full; the solve, which reads each
-// factor entry once, is one thread per state and bound by HBM.
+// number of active lanes, so the factorisations keep the lanes full: each
+// block holds up to four states' matrices in shared memory and spreads their
+// trailing updates over all its threads.  The solves, which read each factor
+// entry once, are one thread per state and bound by memory.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -101,9 +101,9 @@ constexpr long long kAbsMask = 0x7fffffffffffffffLL;
 constexpr long long kDblMinBits = 0x0010000000000000LL;  // bits of DBL_MIN
 
 // S consecutive states per block (4, or 2 or 1 where four matrices do not fit
-// in shared memory) of 32 S threads, each matrix in shared memory with an odd
-// row pitch (a column read by 32 lanes is free of bank conflicts).  Step k:
-// warp w alone works on state w - the pivot (first largest |a|, compared as
+// in shared memory) of 32 S kWarpsPerState threads, each matrix in shared
+// memory with an odd row pitch (a column read by 32 lanes is free of bank
+// conflicts).  Step k: warp w < S alone works on state w - the pivot (first largest |a|, compared as
 // integer bit patterns, no FP64 instruction), the multiplier column scaled by
 // the reciprocal (read through the interchange) and the interchange of the
 // other columns of rows k and p; after a barrier every thread updates one
@@ -252,8 +252,8 @@ struct LuPlanView {
 inline int plan_factor_ints(const LuPlanView& v) { return 3 * v.nn + 2 + v.nR + v.nC; }
 
 // S consecutive states per block (4, or 2 or 1 where four matrices do not fit
-// in shared memory), eliminated in lockstep by 32 S threads: in loads,
-// stores and scalings each thread serves one state, so F-order loads cover
+// in shared memory), eliminated in lockstep by 32 S kWarpsPerState threads:
+// in loads, stores and scalings each thread serves one state, so F-order loads cover
 // whole 32-byte sectors; in the update each thread takes one pattern position
 // for all S states, so one index lookup and one barrier pair serve S states.
 constexpr int kLusMaxStates = 4;
