@@ -493,6 +493,11 @@ def main():
                 "binding": "fp64 pipe: see fp64.pipe_frac (FP64 instructions x rate / DFMA rate)",
                 "fp64": fp64}
 
+    # the device-timed leg is done: its output goes back to the pool, so the
+    # kernel object below sizes its chunks against what the device really has
+    del out
+    torch.cuda.empty_cache()
+
     # end to end through the reference-facing kernel object, host buffers (pinned)
     e2e = None
     if not args.no_e2e and args.kernel != "vjp":
@@ -533,15 +538,11 @@ def main():
 
     implicit = None
     if not args.no_implicit and args.kernel == "jacobian" and nn <= 169:
-        del out
-        torch.cuda.empty_cache()
-        out = None
         implicit = implicit_bench(mech, ev, dev, n, args.order, args.steps, args.warmup,
                                   fp64_peak.value)
 
     sur = None
     if not args.no_surrogate and args.kernel == "jacobian" and args.mech == "gri30":
-        del out
         torch.cuda.empty_cache()
         sur = surrogate_bench(mech, ev, dev, args.sur_train, args.sur_epochs, args.sur_eval,
                               log=lambda h: print(json.dumps(h), file=sys.stderr))

@@ -918,13 +918,27 @@ int pjg_kernel_resize(pjg_kernel* k, size_t problem_size, size_t work_size)
     }
     const size_t nn = m->nn;
     const size_t per_state = eval_state_bytes(m, k->kind, k->order == 'F', t);
-    // two waves per chunk, fewer where the ring and working arrays would pass
-    // the kernel object's budget (large mechanisms)
+    // two waves per chunk; where the ring and working arrays of two waves
+    // would pass the kernel object's budget (large mechanisms), as many whole
+    // waves as the budget holds, and at least one wave if half the free
+    // device memory holds it: a launch of part of a wave takes as long as a
+    // whole one (synthetic 500-species sparse C-order Jacobian, 1.37 MB per
+    // state: a third-of-a-wave chunk ran end to end at 48 % of the copy floor)
     const size_t ring_state = kRing * (1 + nn + k->out_per_state) * sizeof(double) + per_state;
-    int64_t chunk = std::min<int64_t>((int64_t)problem_size,
-                                      PJG_CHUNK_WAVES * wave_states(m, PJG_JACOBIAN));
-    if ((size_t)chunk * ring_state > kKernelBudget)
-        chunk = std::max<int64_t>(PJG_BLOCK, (int64_t)(kKernelBudget / ring_state) / PJG_BLOCK * PJG_BLOCK);
+    const int64_t wave = wave_states(m, PJG_JACOBIAN);
+    int64_t chunk = std::min<int64_t>((int64_t)problem_size, PJG_CHUNK_WAVES * wave);
+    if ((size_t)chunk * ring_state > kKernelBudget) {
+        int64_t c = (int64_t)(kKernelBudget / ring_state);
+        if (c >= wave) {
+            c = c / wave * wave;
+        } else {
+            size_t free_b = 0, total_b = 0;
+            if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
+            c = std::max<int64_t>(c, std::min<int64_t>((int64_t)(free_b / 2 / ring_state), wave));
+        }
+        chunk = std::min<int64_t>((int64_t)problem_size,
+                                  std::max<int64_t>(PJG_BLOCK, c / PJG_BLOCK * PJG_BLOCK));
+    }
     if (chunk == k->chunk && k->d_phi[0]) {
         k->problem_size = problem_size;
         return 0;

@@ -340,3 +340,39 @@ def test_pywrap_kernel_registered_host_arrays(cuda_device):
     del hP, hx, hout
     gc.collect()
     assert not pkg("hostmem")._keep
+
+
+def test_pywrap_kernel_large_mechanism_whole_wave_chunks(cuda_device):
+    """The kernel object for the 500-species mechanism's sparse C-order
+    Jacobian: 1.37 MB of ring and working arrays per state put two waves past
+    its 32 GiB budget, so it takes one whole wave per chunk when half the free
+    device memory holds it (else what the budget holds).  90,000 states span
+    more than one wave; states on both sides of every possible chunk boundary
+    must match the oracle."""
+    import torch
+    torch.cuda.empty_cache()
+    mech = load_mech("synthetic500")
+    n = 90000
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=51)
+    mod = pkg("api").pywrap(mech, order="C", jac_format="sparse")
+    k = mod.PyJacobianKernel(n, 1)
+    ev = evaluator("synthetic500")
+    nnz = ev.nnz
+    out = np.empty(n * nnz)
+    k(P, phi, out)
+    k.close()
+    bounds = set()
+    for c in (77824, 25344, 25088, 24576):
+        bounds.update(range(c, n, c))
+    pick = np.unique(np.concatenate([np.r_[0:8, n - 8:n]] +
+                                    [np.r_[b - 4:b + 4] for b in sorted(bounds)]))
+    pick = pick[(pick >= 0) & (pick < n)]
+    J = out.reshape(n, nnz)[pick]
+    Jref = oracle_mod().Oracle(mech).jacobian(P[pick], phi[pick])
+    ptr, ind = ev.jacobian_indices("C")
+    rows = np.repeat(np.arange(mech.nn), np.diff(ptr))
+    ref = Jref[:, rows, ind]
+    scale = np.abs(Jref).max(axis=2)[:, rows]
+    scale[scale == 0] = 1.0
+    assert np.isfinite(J).all()
+    assert (np.abs(J - ref) / scale).max() < RTOL_JAC
