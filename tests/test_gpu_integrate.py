@@ -332,3 +332,42 @@ def test_jacobian_rates_one_pass_bitwise(cuda_device, order, fmt, name):
     r0 = ev.species_rates(Pd, phid, order=order)
     assert torch.equal(J1, J0)
     assert torch.equal(dphi, r0)
+
+
+@pytest.mark.parametrize("lu_kind", ["pivoting", "sparse"])
+@pytest.mark.parametrize("name", ["h2o2", "gri30"])
+def test_ros2_step_constant_volume_bitwise(cuda_device, lu_kind, name):
+    """Constant volume (param = V, phi_1 = P): the step equals the oracle's
+    factorisation, solves and stage arithmetic applied to this library's own
+    constant-volume rates and Jacobian, bit for bit."""
+    import torch
+    orc = oracle_mod()
+    integ = pkg("integrate")
+    mech = load_mech(name)
+    n = 300
+    V, phi = pkg("states").draw_states(mech.n_species, n, seed=33, x_floor=1e-12, conp=False)
+    h = 10.0 ** np.random.default_rng(8).uniform(-10, -7, n)
+    ev = pkg("api").Evaluator(mech)
+    Vd, hd = torch.from_numpy(V).to(cuda_device), torch.from_numpy(h).to(cuda_device)
+    phid = _to_dev_vec(phi, "F", cuda_device)
+
+    def rates(y):
+        return _from_dev_vec(ev.species_rates(Vd, _to_dev_vec(y, "F", cuda_device), order="F",
+                                              conp=False), "F")
+
+    J = _from_dev_mat(ev.jacobian(Vd, phid, order="F", conp=False), "F")
+    if lu_kind == "pivoting":
+        lu, piv, info_ref = orc.lu_factor(J, integ.ROS2_GAMMA, h)
+        solve = lambda b: orc.lu_solve(lu, piv, b)
+    else:
+        plan = _plan(mech)
+        lu, info_ref = orc.lu_factor_sparse(J, integ.ROS2_GAMMA, h, plan)
+        solve = lambda b: orc.lu_solve_sparse(lu, b, plan)
+    k1 = solve(rates(phi))
+    k2 = solve(orc.ros2_combine(1, h, rates(orc.ros2_combine(0, h, phi, k1)), k1))
+    ref, err_ref = orc.ros2_combine(2, h, phi, k1, k2)
+    st = integ.Ros2Stepper(ev, n, order="F", lu_kind=lu_kind)
+    out, err, info = st.step(Vd, phid, hd, conp=False)
+    assert np.array_equal(info.cpu().numpy(), info_ref)
+    assert np.array_equal(_from_dev_vec(out, "F"), ref)
+    assert np.array_equal(_from_dev_vec(err, "F"), err_ref)
