@@ -76,3 +76,24 @@ def test_product_path_has_no_cpu_fallback(monkeypatch, tmp_path):
     monkeypatch.setattr(L, "library_path", lambda: str(tmp_path / "missing.so"))
     with pytest.raises(RuntimeError):
         pkg("api").Evaluator(load_mech("h2o2"))
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/pyjac_gb300.h is usable from C (C99, pedantic, warnings as
+    errors) and from C++: the boundary has no C++-only syntax."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    src = tmp_path / "use.c"
+    src.write_text('#include "pyjac_gb300.h"\n'
+                   'int main(void) { pjg_mech* m = 0; int32_t ns = 0;\n'
+                   '  return pjg_mech_info(m, &ns, 0, 0) == PJG_OK; }\n')
+    inc = os.path.join(ROOT, "include")
+    for cmd in (["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror"],
+                ["g++", "-std=c++11", "-Wall", "-Wextra", "-Werror", "-x", "c++"]):
+        if shutil.which(cmd[0]) is None:
+            continue
+        r = subprocess.run(cmd + ["-I", inc, "-c", str(src), "-o", str(tmp_path / "use.o")],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
