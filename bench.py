@@ -54,9 +54,9 @@ def pkg(sub=None):
     return importlib.import_module(PKG + ("." + sub if sub else ""))
 
 
-def load_gri():
+def load_gri(jac_type="exact"):
     return pkg().load_mechanism(os.path.join(ROOT, "data", "grimech30.inp"),
-                                os.path.join(ROOT, "data", "thermo30.dat"))
+                                os.path.join(ROOT, "data", "thermo30.dat"), jac_type=jac_type)
 
 
 # --mech: the benchmark configurations' mechanisms, their label and the
@@ -68,17 +68,17 @@ MECHS = {
 }
 
 
-def load_mech(name):
+def load_mech(name, jac_type="exact"):
     if name == "gri30":
-        return load_gri()
+        return load_gri(jac_type)
     if name == "h2o2":
-        return pkg().load_mechanism(os.path.join(ROOT, "data", "h2o2.inp"))
+        return pkg().load_mechanism(os.path.join(ROOT, "data", "h2o2.inp"), jac_type=jac_type)
     import tempfile
     path = os.path.join(tempfile.gettempdir(), "pyjac_gb300_synthetic500_seed0.inp")
     if not os.path.exists(path):
         pkg("mech.synthetic").write(path + ".tmp")  # defaults: 500 species, 2,500 reactions
         os.replace(path + ".tmp", path)
-    return pkg().load_mechanism(path)
+    return pkg().load_mechanism(path, jac_type=jac_type)
 
 
 class ClockSampler(object):
@@ -378,6 +378,9 @@ def main():
     ap.add_argument("--sur-train", type=int, default=1 << 22)
     ap.add_argument("--sur-epochs", type=int, default=12)
     ap.add_argument("--sur-eval", type=int, default=1 << 22)
+    ap.add_argument("--jac-type", default="exact", choices=["exact", "approximate"],
+                    help="Jacobian type: exact (headline) or the reference's approximate type, "
+                         "without the bath-gas terms")
     ap.add_argument("--mech", default="gri30", choices=sorted(MECHS),
                     help="mechanism: GRI-Mech 3.0 (headline), H2/O2, or the 500-species synthetic")
     ap.add_argument("--kernel", default="jacobian", choices=sorted(KERNELS),
@@ -400,7 +403,7 @@ def main():
     lib = pkg("_lib")
     api = pkg("api")
     states = pkg("states")
-    mech = load_mech(args.mech)
+    mech = load_mech(args.mech, args.jac_type)
     ev = api.Evaluator(mech)
     n = args.states
     nn = mech.nn
@@ -552,15 +555,17 @@ def main():
                 "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic",
-                "config": {"workload": ("%s %s FP64 Jacobian, %s order, %d states"
+                "config": {"workload": ("%s %s FP64 %sJacobian, %s order, %d states"
                                         % (label, "dense" if args.format == "full" else
                                            ("sparse CCS" if args.order == "F" else "sparse CRS"),
+                                           "approximate " if args.jac_type == "approximate" else "",
                                            args.order, n)) if args.kernel == "jacobian" else
                            ("%s FP64 %s, %s order, %d states"
                             % (label, "species rates" if args.kernel == "rates" else "J^T v",
                                args.order, n)),
                            "mechanism": MECHS[args.mech][2],
                            "states": n, "order": args.order, "jac_format": args.format,
+                           "jac_type": args.jac_type,
                            "conp": True,
                            "l2": "inputs %.0f MB and outputs %.0f MB, both larger than L2 (126 MB): "
                                  "no flush" % (8e-6 * n_in * n, 8e-6 * n_out * n)},
