@@ -237,7 +237,8 @@ int pjg_write_initial_conditions(const char* filename, int64_t n, int32_t nn, ch
  * ties; symmetric permutation perm[position] = variable) and factored
  * symbolically; step k then updates only the filled pattern's rows x
  * columns.  pjg_lu_symbolic: that order and the counts (FMAs per state,
- * entries of L + U) for a CRS pattern, host only.  pjg_lu_plan_info: the same
+ * entries of L + U) for a CRS pattern, host only, any nn up to 4,096 (to
+ * size larger mechanisms' factorisations; the kernels take nn <= 169).  pjg_lu_plan_info: the same
  * for a mechanism (the plan is built on first use and kept with it).
  * pjg_lu_factor_sparse: M_i = I - s h_i J_i as for pjg_lu_factor, factored
  * without interchanges in the permuted order: lu[i][r][c] (dense layout of

@@ -779,11 +779,12 @@ extern "C" int pjg_internal_lu_solve_sparse(const void* p, int64_t n, char order
     return 0;
 }
 
-// host only: the Markowitz order and the counts of a pattern (no device work)
+// host only: the Markowitz order and the counts of a pattern (no device work;
+// any nn up to 4,096, beyond what the factorisation kernels take)
 extern "C" int pjg_lu_symbolic(int32_t nn, const int32_t* row_ptr, const int32_t* col_ind, int32_t* perm,
                                int32_t* nnz_lu, int64_t* fma)
 {
-    if (nn < 1 || nn > kLuMaxNN) return pjg_internal_fail(PJG_ERR_UNSUPPORTED, "LU: nn must be in [1, 169]");
+    if (nn < 1 || nn > 4096) return pjg_internal_fail(PJG_ERR_UNSUPPORTED, "LU symbolic: nn must be in [1, 4096]");
     if (!row_ptr || !col_ind) return pjg_internal_fail(PJG_ERR_ARG, "null array");
     std::vector<int> pv, tab;
     long long f = 0;

@@ -187,3 +187,17 @@ def test_ros2_sparse_lu_converges_at_second_order():
         errs.append((np.abs(y[0] - ref) / scale).max())
     rates = [errs[i] / errs[i + 1] for i in range(2)]
     assert all(3.0 < r < 5.5 for r in rates), (errs, rates)
+
+
+def test_lu_symbolic_large_mechanism():
+    """The host symbolic analysis sizes mechanisms beyond the factorisation
+    kernels' NN <= 169: the 500-species benchmark mechanism fills to 205,216
+    L + U entries and 28.9M FMAs per state, as the oracle's restatement
+    finds."""
+    orc = oracle_mod()
+    mech = load_mech("synthetic500")
+    pk = pkg("pack").PackedTables(mech)
+    perm, nnz, fma = pkg("integrate").lu_symbolic(pk.crs_row_ptr, pk.crs_col_ind)
+    plan = orc.lu_plan(pk.crs_row_ptr, pk.crs_col_ind)
+    assert np.array_equal(perm, plan["perm"])
+    assert (nnz, fma) == (plan["nnz_lu"], plan["fma"]) == (205216, 28893626)
