@@ -195,3 +195,47 @@ class Ros2Stepper(object):
             self.lu.data_ptr(), None if self.piv is None else self.piv.data_ptr(),
             self.vec.data_ptr(), self.info.data_ptr(), st))
         return out, err, self.info[:n]
+
+
+def integrate_ros2(evaluator, param, phi, t_end, h0=1e-8, rtol=1e-6, atol=1e-12, order="C",
+                   conp=True, lu_kind="pivoting", max_steps=100000, stepper=None):
+    """Integrate every state from t = 0 to t_end with ROS2 steps of its own
+    size, controlled by the embedded first-order error estimate.
+
+    A state's step is accepted when max_j |err_j| / (atol + rtol max(|y_j|,
+    |y_new_j|)) <= 1; its next step is h * min(5, max(0.2, 0.9 / sqrt(e))) (the
+    estimate is O(h^2)), cut to reach t_end exactly.  States that have reached
+    t_end take steps of size 0, which leave them unchanged.  Returns
+    (phi at t_end, stats) with stats = dict(steps=..., rejected=...) per state
+    (CPU int64 arrays).  param and phi as for Evaluator; phi is not modified."""
+    n = param.numel()
+    st = stepper or Ros2Stepper(evaluator, n, order=order, lu_kind=lu_kind)
+    dev = phi.device
+    y = phi.clone()
+    t = torch.zeros(n, dtype=torch.float64, device=dev)
+    h = torch.full((n,), float(h0), dtype=torch.float64, device=dev)
+    steps = torch.zeros(n, dtype=torch.int64, device=dev)
+    rejected = torch.zeros(n, dtype=torch.int64, device=dev)
+    y_new = torch.empty_like(y)
+    err = torch.empty_like(y)
+    state_dim = 1 if order == "C" else 0  # the axis that holds one state's variables
+    for _ in range(int(max_steps)):
+        live = t < t_end
+        if not bool(live.any()):
+            break
+        hs = torch.where(live, torch.minimum(h, t_end - t), torch.zeros_like(h))
+        st.step(param, y, hs.contiguous(), conp=conp, out=y_new, err=err)
+        scale = atol + rtol * torch.maximum(y.abs(), y_new.abs())
+        e = (err.abs() / scale).amax(dim=state_dim)
+        e = torch.where(torch.isfinite(e), e, torch.full_like(e, float("inf")))
+        ok = live & (e <= 1.0)
+        acc = ok.unsqueeze(state_dim) if order == "C" else ok.unsqueeze(0)
+        y = torch.where(acc, y_new, y)
+        t = torch.where(ok, t + hs, t)
+        steps += ok.to(torch.int64)
+        rejected += (live & ~ok).to(torch.int64)
+        fac = torch.clamp(0.9 / torch.sqrt(torch.clamp(e, min=1e-10)), 0.2, 5.0)
+        h = torch.where(live, hs * fac, h)
+    else:
+        raise RuntimeError("integrate_ros2: max_steps reached before t_end")
+    return y, {"steps": steps.cpu().numpy(), "rejected": rejected.cpu().numpy()}

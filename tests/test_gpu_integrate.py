@@ -371,3 +371,64 @@ def test_ros2_step_constant_volume_bitwise(cuda_device, lu_kind, name):
     assert np.array_equal(info.cpu().numpy(), info_ref)
     assert np.array_equal(_from_dev_vec(out, "F"), ref)
     assert np.array_equal(_from_dev_vec(err, "F"), err_ref)
+
+
+_PREMIX_T = (1000.0, 1100.0, 1200.0, 1300.0)
+_PREMIX_T_END = 2e-5
+_premix_refs = {}
+
+
+def _premix_reference(T):
+    """Radau (rtol 1e-13) end state of the oracle's ODE for the premix at T."""
+    if T not in _premix_refs:
+        from scipy.integrate import solve_ivp
+        from test_integrate_oracle import premix_h2o2
+        mech, P, phi = premix_h2o2(T=T)
+        o = oracle_mod().Oracle(mech)
+        _premix_refs[T] = solve_ivp(lambda t, v: o.species_rates(P, v[None])[0],
+                                    (0, _PREMIX_T_END), phi[0], method="Radau",
+                                    jac=lambda t, v: o.jacobian(P, v[None])[0], rtol=1e-13,
+                                    atol=1e-22).y[:, -1]
+    return _premix_refs[T]
+
+
+@pytest.mark.parametrize("order,lu_kind", [("C", "pivoting"), ("F", "sparse")])
+def test_integrate_ros2_adaptive_premix(cuda_device, order, lu_kind):
+    """Adaptive ROS2 (rtol 1e-5) over 20 us on H2/O2/Ar premixes at four
+    temperatures, each state with its own step sizes: the end states agree
+    with Radau solutions of the oracle's ODE at rtol 1e-13 to 2e-3 of each
+    component's scale."""
+    import torch
+    from test_integrate_oracle import premix_h2o2
+    integ = pkg("integrate")
+    rows = [premix_h2o2(T=T) for T in _PREMIX_T]
+    mech = rows[0][0]
+    P = np.concatenate([r[1] for r in rows])
+    phi = np.concatenate([r[2] for r in rows])
+    ev = pkg("api").Evaluator(mech)
+    y, stats = integ.integrate_ros2(ev, torch.from_numpy(P).to(cuda_device),
+                                    _to_dev_vec(phi, order, cuda_device), _PREMIX_T_END, h0=1e-9,
+                                    rtol=1e-5, atol=1e-16, order=order, lu_kind=lu_kind)
+    y = _from_dev_vec(y, order)
+    assert (stats["steps"] > 0).all()
+    for i, T in enumerate(_PREMIX_T):
+        ref = _premix_reference(T)
+        scale = np.abs(ref) + 1e-8 * np.abs(ref).max()
+        assert (np.abs(y[i] - ref) / scale).max() < 2e-3, (T, stats)
+
+
+def test_integrate_ros2_radical_rich_states(cuda_device):
+    """Radical-rich random GRI states over 10 ns from a first step of 100 ns,
+    so that steps are rejected: every state reaches t_end with finite
+    values."""
+    import torch
+    integ = pkg("integrate")
+    mech = load_mech("gri30")
+    n = 64
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=71, x_floor=1e-12)
+    ev = pkg("api").Evaluator(mech)
+    y, stats = integ.integrate_ros2(ev, torch.from_numpy(P).to(cuda_device),
+                                    torch.from_numpy(phi).to(cuda_device), 1e-8, h0=1e-7,
+                                    rtol=1e-4, atol=1e-14)
+    assert np.isfinite(y.cpu().numpy()).all()
+    assert (stats["steps"] > 0).all() and stats["rejected"].sum() > 0
