@@ -13,6 +13,10 @@ solvers (KPP): rows and columns ordered once by the Markowitz rule on the
 mechanism's Jacobian pattern, no interchanges, only the filled pattern
 updated (GRI-Mech 3.0: 19,752 FMAs per state instead of 51,039).
 
+On top of the step, integrate_ros2 advances every state to a common end time
+with its own adaptive step sizes (the control runs as a few element-wise
+tensor operations per step; the step itself is the library's).
+
 Layouts are the dense Jacobian's: order 'C' — jac and lu (N, NN, NN)
 [state, row, col]; order 'F' — (NN, NN, N) [col, row, state].  Vectors and
 pivots are laid out like phi: (N, NN) for 'C', (NN, N) for 'F'.  Step sizes

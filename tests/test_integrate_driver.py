@@ -70,3 +70,20 @@ def test_finished_states_take_zero_steps():
 def test_max_steps_raises():
     with pytest.raises(RuntimeError, match="max_steps"):
         _run([1e9], 1.0, h0=1e-12, rtol=1e-8, atol=1e-30, max_steps=5)
+
+
+def test_entry_points_validate_before_the_library():
+    """Host tensors, wrong dtypes and non-square matrices are refused in
+    Python, before any library call."""
+    integ = pkg("integrate")
+    cpu = torch.zeros((2, 3, 3), dtype=torch.float64)
+    with pytest.raises(TypeError):
+        integ.lu_factor(cpu, 1e-6)
+    with pytest.raises(TypeError):
+        integ.lu_solve(cpu, torch.zeros((2, 3), dtype=torch.int32), torch.zeros((2, 3)))
+    with pytest.raises(ValueError, match="square"):
+        integ._n_of(torch.zeros((2, 3, 4)), "C")
+    with pytest.raises(ValueError, match="dense"):
+        integ._n_of(torch.zeros((2, 3)), "C")
+    with pytest.raises(ValueError):
+        integ.Ros2Stepper.__init__(object.__new__(integ.Ros2Stepper), None, 4, lu_kind="qr")
