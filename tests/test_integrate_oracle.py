@@ -201,3 +201,28 @@ def test_lu_symbolic_large_mechanism():
     plan = orc.lu_plan(pk.crs_row_ptr, pk.crs_col_ind)
     assert np.array_equal(perm, plan["perm"])
     assert (nnz, fma) == (plan["nnz_lu"], plan["fma"]) == (205216, 28893626)
+
+
+def test_ros2_constant_volume_converges_at_second_order():
+    """The same premix at constant volume (param = V = 1 m^3, phi_1 = P): the
+    oracle's ROS2 converges at second order against Radau on the conv ODE."""
+    from scipy.integrate import solve_ivp
+    orc = oracle_mod()
+    mech, P, phi = premix_h2o2()
+    o = orc.Oracle(mech)
+    V = np.array([1.0])
+    phi = phi.copy()
+    phi[0, 1] = P[0]  # phi_1 is the pressure at constant volume
+    t_end = 2e-5
+    ref = solve_ivp(lambda t, v: o.species_rates(V, v[None], conp=False)[0], (0, t_end), phi[0],
+                    method="Radau", jac=lambda t, v: o.jacobian(V, v[None], conp=False)[0],
+                    rtol=1e-13, atol=1e-22).y[:, -1]
+    scale = np.abs(ref) + 1e-8 * np.abs(ref).max()
+    errs = []
+    for steps in (16, 32, 64):
+        y = phi.copy()
+        for _ in range(steps):
+            y, _, info = orc.ros2_step(o, V, y, t_end / steps, conp=False)
+        errs.append((np.abs(y[0] - ref) / scale).max())
+    rates = [errs[i] / errs[i + 1] for i in range(2)]
+    assert all(3.0 < r < 5.5 for r in rates), (errs, rates)
