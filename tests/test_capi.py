@@ -97,3 +97,43 @@ def test_header_is_plain_c(tmp_path):
         r = subprocess.run(cmd + ["-I", inc, "-c", str(src), "-o", str(tmp_path / "use.o")],
                            capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_c_caller_links_and_runs(lib, tmp_path):
+    """A plain C program links against the library and calls host-side entry
+    points (the Markowitz analysis of an arrow pattern, which orders the
+    dense node late and fills nothing; an initial-condition file round
+    trip): the C ABI works without Python."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no gcc")
+    data = tmp_path / "data.bin"
+    src = tmp_path / "main.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "pyjac_gb300.h"
+int main(void) {
+    int32_t row_ptr[5] = {0, 4, 6, 8, 10};
+    int32_t col_ind[10] = {0, 1, 2, 3, 0, 1, 0, 2, 0, 3};
+    int32_t perm[4], nnz = 0; int64_t fma = 0;
+    int rc = pjg_lu_symbolic(4, row_ptr, col_ind, perm, &nnz, &fma);
+    printf("%d %d %d %d %d %d %lld\n", rc, perm[0], perm[1], perm[2], perm[3], nnz, (long long)fma);
+    double param[2] = {101325.0, 2e5}, phi[6] = {1000, 1, 0.1, 1500, 2, 0.2}, p2[2], phi2[6];
+    rc = pjg_write_initial_conditions("%s", 2, 3, 'C', param, phi);
+    rc |= pjg_read_initial_conditions("%s", 2, 3, 'C', p2, phi2);
+    printf("%d %g %g %g\n", rc, p2[1], phi2[3], phi2[5]);
+    return 0;
+}
+'''.replace('"%s"', '"' + str(data) + '"'))
+    build_dir = os.path.dirname(pkg("_lib").library_path())
+    exe = tmp_path / "a.out"
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-L",
+                        build_dir, "-lpyjac_gb300", "-Wl,-rpath," + build_dir, "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.split("\n")
+    assert lines[0].split() == ["0", "1", "2", "0", "3", "10", "3"]
+    assert lines[1].split() == ["0", "200000", "1500", "0.2"]
