@@ -64,7 +64,7 @@ typedef struct pjg_tables {
                               * :4187-4191); the pattern arrays must be the
                               * approximate type's */
     const void* rxn;         /* nr reaction records, 192 bytes each */
-    const double* species;   /* ns species records, 16 doubles each */
+    const double* species;   /* ns species records, 48 doubles each (PJG_SP_DOUBLES) */
     const int32_t* thd_spec; /* third-body species lists */
     const double* thd_coef;  /* efficiency minus flag, aligned with thd_spec */
     int32_t n_thd;           /* length of thd_spec / thd_coef */
@@ -282,24 +282,6 @@ int pjg_host_unregister(void* ptr);
 
 /* Copy the last error message of this thread into buf (always NUL-terminated). */
 int pjg_last_error(char* buf, size_t len);
-
-/* Instrumentation (no reference counterpart; the reference prints wall-clock
- * timings from its generated main, kernel.cpp.in:645-712).
- * pjg_launch_count: GPU kernel launches this library has issued so far.
- * pjg_profile_begin / pjg_profile_end: record CUDA events around every launch
- * of the evaluation kernels between the two calls; end synchronises those
- * events and returns their number and summed duration in milliseconds. */
-int pjg_launch_count(int64_t* count);
-/* Measured dense FP64 FMA throughput of the current device in TFLOP/s (the
- * denominator of the FP64 roofline; runs a ~10 ms probe kernel). */
-int pjg_fp64_peak(double* tflops);
-int pjg_profile_begin(void);
-int pjg_profile_end(int64_t* launches, double* total_ms);
-/* y = exp(x) through the table-driven exponential the evaluation kernels use
- * for rate constants, equilibrium constants and fall-off blending (device
- * pointers, asynchronous on `stream`); exposed so that its error against the
- * CUDA library exp can be measured.  No reference counterpart. */
-int pjg_math_exp(const double* x, double* y, int64_t n, void* stream);
 
 #ifdef __cplusplus
 }

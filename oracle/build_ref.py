@@ -17,6 +17,11 @@ Flags follow the reference's libgen C flags (pyjac/libgen/libgen.py:24-49:
 ``-O3 -fopenmp``), without ``-march=native`` so that the build is portable.
 
 Usage: python oracle/build_ref.py [--reference DIR]
+
+The reference tree is taken from --reference, else from the PYJAC_REFERENCE
+environment variable, else from this recipe's default location
+(``DEFAULT_REFERENCE``, where the reference is mounted in the build
+container).
 """
 import argparse
 import os
@@ -27,6 +32,13 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 MECHS = ("h2o2", "ch4")
+DEFAULT_REFERENCE = "/root/reference"
+
+
+def reference_dir(reference=None):
+    """The reference tree this recipe reads: the argument, else
+    $PYJAC_REFERENCE, else DEFAULT_REFERENCE."""
+    return reference or os.environ.get("PYJAC_REFERENCE") or DEFAULT_REFERENCE
 
 
 def _sizes(exdir):
@@ -90,13 +102,14 @@ def build_from_preprocessed(quiet=True):
     return built
 
 
-def build(reference="/root/reference", quiet=False):
+def build(reference=None, quiet=False):
     """Compile every shipped example; return {mech: path_to_so}.
 
     Also writes oracle/_ref/ref_<mech>.ii, the shim with the example's
     generated code inlined (a build intermediate, not committed),
     so that hosts without the reference tree can build the same library with
     build_from_preprocessed()."""
+    reference = reference_dir(reference)
     if not os.path.isdir(os.path.join(reference, "examples", "opencl")):
         return build_from_preprocessed(quiet)
     os.makedirs(OUT, exist_ok=True)
@@ -133,7 +146,7 @@ def build(reference="/root/reference", quiet=False):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None)
     a = ap.parse_args()
     out = build(a.reference)
     print(out)

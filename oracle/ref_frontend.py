@@ -39,12 +39,32 @@ class _Record(object):
         return type(self)(**d)
 
 
+class _LoopyArg(object):
+    """Stand-in for loopy's kernel-argument classes (ArrayArg, ValueArg,
+    TemporaryVariable ...): keeps the name and keyword arguments, so that the
+    reference's array creator (pyjac/core/array_creator.py creator.__call__
+    :1588-1656) builds real access strings such as 'Pr[j, i + 4]'."""
+
+    def __init__(self, name, *args, **kw):
+        self.name = name
+        self._kw = dict(kw)
+        self.__dict__.update(kw)
+
+    def copy(self, **kw):
+        d = dict(self._kw)
+        d.update(kw)
+        return _LoopyArg(d.pop("name", self.name), **d)
+
+
 class _StubLoader(importlib.abc.Loader):
     def create_module(self, spec):
         m = mock.MagicMock(name=spec.name)
         m.__path__ = []
         m.__spec__ = spec
         m.__name__ = spec.name
+        if spec.name == "loopy":
+            for k in ("ArrayArg", "GlobalArg", "TemporaryVariable", "ValueArg", "ConstantArg"):
+                setattr(m, k, _LoopyArg)
         if spec.name.split(".")[0] == "pytools":
             m.ImmutableRecord = _Record
             m.Record = _Record
@@ -70,13 +90,16 @@ class _StubFinder(importlib.abc.MetaPathFinder):
 _loaded = None
 
 
-def load(reference="/root/reference"):
-    """Return a namespace with the reference's front-end functions."""
+def load(reference=None):
+    """Return a namespace with the reference's front-end functions, imported
+    from the tree at `reference` (default: the PYJAC_REFERENCE environment
+    variable)."""
     global _loaded
     if _loaded is not None:
         return _loaded
-    if not os.path.isdir(os.path.join(reference, "pyjac")):
-        raise RuntimeError("reference tree not found at %s" % reference)
+    reference = reference or os.environ.get("PYJAC_REFERENCE")
+    if not reference or not os.path.isdir(os.path.join(reference, "pyjac")):
+        raise RuntimeError("reference tree not found (%r); set PYJAC_REFERENCE" % reference)
     sys.dont_write_bytecode = True
     sys.meta_path.insert(0, _StubFinder())
     if reference not in sys.path:
@@ -108,6 +131,13 @@ def load(reference="/root/reference"):
     npmod.__dict__.update(np.__dict__)
     npmod.array = _array
     rs.np = npmod
+    # array_creator.py:2354 uses np.in1d, which numpy 2 removed (np.isin is
+    # the same function)
+    arc = importlib.import_module("pyjac.core.array_creator")
+    npc = types.ModuleType("np_in1d")
+    npc.__dict__.update(np.__dict__)
+    npc.in1d = np.isin
+    arc.np = npc
 
     _loaded = types.SimpleNamespace(read_mech=mi.read_mech,
                                     find_last_species=cj.find_last_species,
@@ -115,12 +145,15 @@ def load(reference="/root/reference"):
                                     assign_rates=rs.assign_rates,
                                     determine_jac_inds=cj.determine_jac_inds,
                                     RateSpecialization=en.RateSpecialization,
-                                    JacobianType=en.JacobianType)
+                                    JacobianType=en.JacobianType,
+                                    rate_subs=rs, array_creator=arc,
+                                    loopy_utils=importlib.import_module(
+                                        "pyjac.loopy_utils.loopy_utils"))
     return _loaded
 
 
 def reference_tables(mech, therm=None, last_spec=None, rate_spec="hybrid",
-                     jac_type="exact", reference="/root/reference"):
+                     jac_type="exact", reference=None):
     """Run the reference front end on a Chemkin file; return (specs, reacs, val)."""
     ref = load(reference)
     elems, specs, reacs = ref.read_mech(mech, therm)
@@ -129,3 +162,38 @@ def reference_tables(mech, therm=None, last_spec=None, rate_spec="hybrid",
     val = ref.determine_jac_inds(reacs, specs, getattr(ref.RateSpecialization, rate_spec),
                                  getattr(ref.JacobianType, jac_type))
     return specs, reacs, val
+
+
+def reference_rate_kernels(mech, therm=None, conp=True, reference=None, test_size=16):
+    """The reference's own instruction text of the species-rate sub-kernels
+    whose forms no shipped kernel exercises, generated by its generators
+    (pyjac/core/rate_subs.py) for a Chemkin file, C language, C order,
+    hybrid rate specialisation: {name: knl_info} for 'plog'
+    (get_plog_arrhenius_rates :2084), 'cheb' (get_cheb_arrhenius_rates
+    :1904), 'sri' (get_sri_kernel :2472), 'troe' (get_troe_kernel :2350),
+    'extra_var' (get_extra_var_rates :798) and 'temperature'
+    (get_temperature_rate :963), and the reference's rate tables."""
+    ref = load(reference)
+    rs, arc, lu = ref.rate_subs, ref.array_creator, ref.loopy_utils
+    elems, specs, reacs = ref.read_mech(mech, therm)
+    specs = ref.find_last_species(specs)
+    ref.reassign_species_lists(reacs, specs)
+    spec = ref.RateSpecialization.hybrid
+    opts = lu.loopy_options(width=None, depth=None, lang="c", order="C", rate_spec=spec)
+    info = rs.assign_rates(reacs, specs, spec)
+    nst = arc.NameStore(opts, info, conp, test_size)
+    out = {}
+    if info["plog"]["num"]:
+        out["plog"] = rs.get_plog_arrhenius_rates(opts, nst, info["plog"]["max_P"], test_size=test_size)
+    if info["cheb"]["num"]:
+        out["cheb"] = rs.get_cheb_arrhenius_rates(opts, nst, np.max(info["cheb"]["num_P"]),
+                                                  np.max(info["cheb"]["num_T"]), test_size=test_size)
+    for name, fn in (("sri", rs.get_sri_kernel), ("troe", rs.get_troe_kernel)):
+        k = fn(opts, nst, test_size=test_size)
+        if k:
+            out[name] = k
+    out["extra_var"] = rs.get_extra_var_rates(opts, nst, conp=conp, test_size=test_size)
+    out["temperature"] = rs.get_temperature_rate(opts, nst, conp=conp, test_size=test_size)
+    for k, v in list(out.items()):
+        out[k] = v[0] if isinstance(v, list) else v
+    return out, info, specs

@@ -1,6 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Run in a tree where the reference is available (default /root/reference):
+Run in a tree where the reference is available (--reference, else the
+PYJAC_REFERENCE environment variable, else the default of oracle/build_ref.py):
 
     python tests/golden/make_golden.py [--reference DIR]
 
@@ -65,8 +66,10 @@ def flatten(val, prefix=""):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None)
     a = ap.parse_args()
+    build_ref = importlib.import_module("build_ref")
+    a.reference = build_ref.reference_dir(a.reference)
     rf = importlib.import_module("ref_frontend")
     conftest = importlib.import_module("conftest")
     syn = importlib.import_module("pyjac-v2_gb300.mech.synthetic")
@@ -85,11 +88,10 @@ def main():
                                          jac_type="approximate", reference=a.reference)
         np.savez_compressed(os.path.join(HERE, "jacapprox_%s.npz" % name),
                             **flatten(aval["jac_inds"]))
-    build_ref = importlib.import_module("build_ref")
     build_ref.build(a.reference, quiet=True)
     orc = importlib.import_module("oracle")
     states = importlib.import_module("pyjac-v2_gb300.states")
-    for name, shipped, n, floor in (("h2o2", "h2o2", 256, None), ("gri30", "ch4", 64, 1e-12)):
+    for name, shipped, n, floor in (("h2o2", "h2o2", 256, None), ("gri30", "ch4", 1024, 1e-12)):
         ref = orc.RefKernels(shipped)
         P, phi = states.draw_states(ref.ns, n, seed=2024, x_floor=floor)
         phiF = np.ascontiguousarray(phi.T)

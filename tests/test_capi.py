@@ -1,6 +1,7 @@
 """C ABI checks that need no GPU: the library builds, loads, exports every
-function include/pyjac_gb300.h declares, and rejects bad arguments with an
-error status (never an abort) before touching the device."""
+function include/*.h declares (the boundary, pyjac_gb300.h, and the
+instrumentation hooks, pyjac_gb300_internal.h), and rejects bad arguments
+with an error status (never an abort) before touching the device."""
 import ctypes
 import os
 import re
@@ -11,9 +12,11 @@ import pytest
 from conftest import ROOT, load_mech, pkg
 
 
-def declared_functions():
-    with open(os.path.join(ROOT, "include", "pyjac_gb300.h")) as fh:
-        text = fh.read()
+def declared_functions(headers=("pyjac_gb300.h", "pyjac_gb300_internal.h")):
+    text = ""
+    for h in headers:
+        with open(os.path.join(ROOT, "include", h)) as fh:
+            text += fh.read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\bint\s+(pjg_\w+)\s*\(", text)))
 
@@ -31,6 +34,15 @@ def test_exports_every_declared_symbol(lib):
         assert hasattr(lib, n), n
     bound = {s[0] for s in pkg("_lib").SIGNATURES}
     assert set(names) <= bound
+
+
+def test_instrumentation_hooks_are_not_in_the_boundary_header():
+    """Bench and test hooks live in the internal header only."""
+    public = set(declared_functions(("pyjac_gb300.h",)))
+    internal = set(declared_functions(("pyjac_gb300_internal.h",)))
+    assert internal == {"pjg_launch_count", "pjg_fp64_peak", "pjg_profile_begin",
+                        "pjg_profile_end", "pjg_math_exp", "pjg_eval_chunk"}
+    assert not public & internal
 
 
 def test_bad_arguments_return_status(lib):
@@ -79,16 +91,16 @@ def test_product_path_has_no_cpu_fallback(monkeypatch, tmp_path):
 
 
 def test_header_is_plain_c(tmp_path):
-    """include/pyjac_gb300.h is usable from C (C99, pedantic, warnings as
+    """include/pyjac_gb300.h (and the internal header) is usable from C (C99, pedantic, warnings as
     errors) and from C++: the boundary has no C++-only syntax."""
     import shutil
     import subprocess
     if shutil.which("gcc") is None:
         pytest.skip("no gcc")
     src = tmp_path / "use.c"
-    src.write_text('#include "pyjac_gb300.h"\n'
-                   'int main(void) { pjg_mech* m = 0; int32_t ns = 0;\n'
-                   '  return pjg_mech_info(m, &ns, 0, 0) == PJG_OK; }\n')
+    src.write_text('#include "pyjac_gb300.h"\n#include "pyjac_gb300_internal.h"\n'
+                   'int main(void) { pjg_mech* m = 0; int32_t ns = 0; int64_t c = 0;\n'
+                   '  return pjg_mech_info(m, &ns, 0, 0) == PJG_OK && pjg_launch_count(&c) == 0; }\n')
     inc = os.path.join(ROOT, "include")
     for cmd in (["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror"],
                 ["g++", "-std=c++11", "-Wall", "-Wextra", "-Werror", "-x", "c++"]):

@@ -72,6 +72,15 @@ def test_max_steps_raises():
         _run([1e9], 1.0, h0=1e-12, rtol=1e-8, atol=1e-30, max_steps=5)
 
 
+def test_exactly_max_steps_is_not_a_failure():
+    # the slow state reaches t_end in one accepted step (h0 = t_end), so a
+    # step cap of exactly one is enough and must not raise
+    y0, y, stats, st = _run([1.0], 1e-3, h0=1e-3, rtol=1e-3, atol=1e-30, max_steps=1)
+    assert stats["steps"][0] == 1 and st.calls == 1
+    assert torch.allclose(y, torch.exp(torch.tensor(-1e-3, dtype=torch.float64)) * y0,
+                          rtol=1e-12, atol=0)
+
+
 def test_entry_points_validate_before_the_library():
     """Host tensors, wrong dtypes and non-square matrices are refused in
     Python, before any library call."""
