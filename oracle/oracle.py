@@ -21,6 +21,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 SRC = os.path.join(HERE, "pyjac_oracle.c")
 HDR = os.path.join(HERE, "pyjac_oracle.h")
+COUNT_SRC = os.path.join(HERE, "flop_count.cpp")
+COUNT_LIB = os.path.join(BUILD, "liboracle_count.so")
 
 
 def build(force=False, quiet=True):
@@ -35,6 +37,25 @@ def build(force=False, quiet=True):
     subprocess.check_call(cmd)
     os.replace(LIB + ".tmp", LIB)
     return LIB
+
+
+def build_counter(force=False, quiet=True):
+    """The operation-counting build of the same oracle source (flop_count.cpp)."""
+    os.makedirs(BUILD, exist_ok=True)
+    deps = [SRC, HDR, COUNT_SRC]
+    if (not force and os.path.exists(COUNT_LIB) and
+            os.path.getmtime(COUNT_LIB) >= max(os.path.getmtime(d) for d in deps)):
+        return COUNT_LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-w", "-ffp-contract=off", "-I", HERE,
+           COUNT_SRC, "-o", COUNT_LIB + ".tmp", "-lm"]
+    if not quiet:
+        print(" ".join(cmd))
+    subprocess.check_call(cmd)
+    os.replace(COUNT_LIB + ".tmp", COUNT_LIB)
+    return COUNT_LIB
+
+
+OP_NAMES = ("add", "mul", "div", "fma", "minmax", "exp", "log", "log10", "pow", "sqrt")
 
 
 _I = ctypes.POINTER(ctypes.c_int)
@@ -173,6 +194,53 @@ class Oracle(object):
                 phi.ctypes.data_as(_D), out.ctypes.data_as(_D), int(nthreads))
         if rc != 0:
             raise RuntimeError("oracle returned %d" % rc)
+        return out
+
+    def op_counts(self, param, phi, kind="jacobian", conp=True):
+        """FP64 operations of the reference's formulation per state, averaged
+        over the given states (C order): dict of OP_NAMES -> count and
+        'flops' = add + mul + div + 2 fma (flop_count.cpp)."""
+        lib = getattr(self, "_count_lib", None)
+        if lib is None:
+            lib = self._count_lib = ctypes.CDLL(build_counter())
+            lib.orc_count_ops.restype = ctypes.c_int
+            lib.orc_count_ops.argtypes = [ctypes.POINTER(_OrcMech), ctypes.c_int, ctypes.c_long,
+                                          ctypes.c_int, _D, _D, ctypes.POINTER(ctypes.c_longlong)]
+        param = np.ascontiguousarray(param, dtype=np.float64)
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        n = phi.shape[0]
+        c = (ctypes.c_longlong * len(OP_NAMES))()
+        rc = lib.orc_count_ops(ctypes.byref(self._m), {"rates": 0, "jacobian": 1}[kind], n,
+                               int(bool(conp)), param.ctypes.data_as(_D), phi.ctypes.data_as(_D), c)
+        if rc != 0:
+            raise RuntimeError("orc_count_ops returned %d" % rc)
+        out = {k: c[i] / n for i, k in enumerate(OP_NAMES)}
+        out["flops"] = out["add"] + out["mul"] + out["div"] + 2 * out["fma"]
+        return out
+
+    def rates_detail(self, param, phi, conp=True):
+        """Per state intermediates of the species rates (orc_rates_detail):
+        dict of kf, kr (n, nr), Pr, Fi (n, n_fall), wdot, conc (n, ns), dphi
+        (n, NN)."""
+        fn = self._lib.orc_rates_detail
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.POINTER(_OrcMech), ctypes.c_int, ctypes.c_double, _D] + [_D] * 7
+        param = np.ascontiguousarray(param, dtype=np.float64)
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        n, nr, ns = phi.shape[0], self.mech.val["Nr"], self.nn - 1
+        nf = max(int(self.mech.val["fall"]["num"]), 1)
+        out = {"kf": np.empty((n, nr)), "kr": np.empty((n, nr)), "Pr": np.empty((n, nf)),
+               "Fi": np.empty((n, nf)), "wdot": np.empty((n, ns)), "dphi": np.empty((n, ns + 1)),
+               "conc": np.empty((n, ns))}
+        for s in range(n):
+            row = {k: np.empty(v.shape[1]) for k, v in out.items()}
+            rc = fn(ctypes.byref(self._m), int(bool(conp)), float(param[s]), phi[s].ctypes.data_as(_D),
+                    *[row[k].ctypes.data_as(_D) for k in ("kf", "kr", "Pr", "Fi", "wdot", "dphi",
+                                                          "conc")])
+            if rc != 0:
+                raise RuntimeError("oracle returned %d" % rc)
+            for k in out:
+                out[k][s] = row[k]
         return out
 
     def species_rates(self, param, phi, conp=True, nthreads=0):

@@ -78,6 +78,12 @@ int orc_jacobian(const orc_mech* m, long n, int conp, const double* param,
  * absolute values (sum |nu| (|rop_f| + |rop_r|) |ci| per species, propagated
  * through the T and extra-variable rates).  A parity metric, not a reference
  * quantity. */
+/* One state's intermediates of the species-rate evaluation: forward and
+ * reverse rate constants (nr each), reduced pressures and blending factors
+ * (one per fall-off reaction), net molar production rates (ns), dphi
+ * (ns + 1) and concentrations (ns).  Any output may be NULL. */
+int orc_rates_detail(const orc_mech* m, int conp, double param, const double* phi, double* kf,
+                     double* kr, double* Pr, double* Fi, double* wdot, double* dphi, double* conc);
 int orc_rates_scale(const orc_mech* m, long n, int conp, const double* param,
                     const double* phi, double* scale, int nthreads);
 /* Species thermo of the chem_utils kernel type (rate_subs.py write_chem_utils

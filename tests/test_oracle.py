@@ -121,3 +121,103 @@ def test_oracle_approximate_jacobian_drops_only_bath_gas_terms(name):
     assert (Ja[:, ~mask] == 0).all()
     if name in ("h2o2", "gri30"):  # mechanisms with bath-gas reactions
         assert np.abs(d[:, :, 2:]).max() > 0
+
+
+def test_op_counter_is_pinned_and_stored():
+    """The FP64 operation counter (oracle/flop_count.cpp, the oracle's source
+    compiled with a counting double) reproduces the committed per-state
+    counts of data/fp64_op_counts.json, which bench.py uses for the FP64
+    roofline; a rebuilt count of H2/O2 and GRI-Mech 3.0 equals them."""
+    import importlib
+    import json
+    import sys
+    from conftest import ROOT
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    cf = importlib.import_module("count_flops")
+    with open(os.path.join(ROOT, "data", "fp64_op_counts.json")) as fh:
+        stored = json.load(fh)["mechanisms"]
+    for name in ("h2o2", "gri30"):
+        fresh = cf.count(name)
+        for kind in ("rates", "jacobian", "vjp"):
+            assert fresh[kind] == stored[name][kind], (name, kind)
+    g = stored["gri30"]
+    # the Jacobian carries the rates' work plus its derivative blocks
+    assert g["jacobian"]["flops"] > 5 * g["rates"]["flops"]
+    assert g["rates"]["exp"] >= 325  # at least one exponential per reaction
+
+
+def test_op_counter_leaves_the_arithmetic_unchanged():
+    """The counting build evaluates the same IEEE operations as the plain
+    oracle: the counts are of the arithmetic the oracle's results come from."""
+    import ctypes
+    mech = load_mech("h2o2")
+    orc = oracle_mod()
+    o = orc.Oracle(mech)
+    states = __import__("conftest").pkg("states")
+    P, phi = states.draw_states(mech.n_species, 16, seed=5, x_floor=1e-12)
+    ref = o.jacobian(P, phi)
+    o.op_counts(P, phi, "jacobian")  # loads the counting library
+    lib = o._count_lib
+    # the counting library exports the plain entry points of the same source
+    fn = lib.orc_jacobian
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(orc._OrcMech), ctypes.c_long, ctypes.c_int] + [orc._D] * 3 + [ctypes.c_int]
+    out = np.empty_like(ref)
+    P = np.ascontiguousarray(P)
+    phi = np.ascontiguousarray(phi)
+    assert fn(ctypes.byref(o._m), 16, 1, P.ctypes.data_as(orc._D), phi.ctypes.data_as(orc._D),
+              out.ctypes.data_as(orc._D), 1) == 0
+    assert np.array_equal(out, ref)
+
+
+def test_oracle_matches_reference_kernel_text_forms():
+    """The forms no shipped kernel runs (PLOG, Chebyshev, SRI and Troe
+    blending, dT/dt and the extra-variable rate at constant pressure and
+    constant volume) against the reference's own generated kernel text,
+    executed on the same states (tests/golden/ref_forms_testmech.npz, made by
+    tests/golden/make_ref_forms.py): the oracle's intermediates agree to
+    1e-13, with the kernels' inputs equal to the stored ones."""
+    g = np.load(os.path.join(GOLDEN, "ref_forms_testmech.npz"))
+    mech = load_mech("testmech")
+    o = oracle_mod().Oracle(mech)
+
+    def rel(a, b):
+        return float((np.abs(a - b) / np.maximum(np.abs(b), 1e-300)).max())
+
+    for tag, conp in (("conp", True), ("conv", False)):
+        P, phi = g[tag + "/P"], g[tag + "/phi"]
+        # the fixture reaches the guards and the tables' ends
+        assert phi[:, 0].min() < 100.0 and phi[:, 0].max() > 10000.0
+        d = o.rates_detail(P, phi, conp=conp)
+        assert np.array_equal(d["Pr"], g[tag + "/in_Pr"])
+        assert np.array_equal(d["wdot"], g[tag + "/in_wdot"])
+        assert rel(d["kf"][:, g["plog_map"]], g[tag + "/ref_plog"]) <= 1e-13
+        assert rel(d["kf"][:, g["cheb_map"]], g[tag + "/ref_cheb"]) <= 1e-13
+        for form in ("sri", "troe"):
+            m = g[form + "_map"]
+            assert m.size and rel(d["Fi"][:, m], g[tag + "/ref_" + form][:, m]) <= 1e-13, form
+        assert rel(d["dphi"][:, 0], g[tag + "/ref_temperature"][:, 0]) <= 1e-13
+        assert rel(d["dphi"][:, 1], g[tag + "/ref_extra_var"][:, 1]) <= 1e-13
+    texts = "\n".join(str(t) for t in g["conv/texts"])
+    assert "pow(" in texts and "cheb_params" in texts and "plog_params" in texts
+
+
+@pytest.mark.skipif(not os.environ.get("PYJAC_REFERENCE"), reason="PYJAC_REFERENCE not set")
+def test_reference_form_fixture_regenerates():
+    """With the reference tree at hand, its generators' text executed again
+    gives the stored golden values bit for bit."""
+    import importlib
+    import sys
+    from conftest import ROOT
+    for p in (os.path.join(ROOT, "tests", "golden"), os.path.join(ROOT, "oracle")):
+        sys.path.insert(0, p)
+    mk = importlib.import_module("make_ref_forms")
+    rf = importlib.import_module("ref_frontend")
+    g = np.load(os.path.join(GOLDEN, "ref_forms_testmech.npz"))
+    mech = load_mech("testmech")
+    o = oracle_mod().Oracle(mech)
+    for tag, conp in (("conp", True), ("conv", False)):
+        knls, info, _ = rf.reference_rate_kernels(mk.MECH, conp=conp)
+        res = mk.run_forms(knls, info, mech, o, conp)
+        for k, v in res.items():
+            assert np.array_equal(v, g[tag + "/" + k]), (tag, k)
