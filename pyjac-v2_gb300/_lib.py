@@ -69,6 +69,8 @@ SIGNATURES = [
     ("pjg_profile_end", ctypes.c_int, [ctypes.POINTER(ctypes.c_int64),
                                        ctypes.POINTER(ctypes.c_double)]),
     ("pjg_math_exp", ctypes.c_int, [_VP, _VP, ctypes.c_int64, _VP]),
+    ("pjg_eval_chunk", ctypes.c_int,
+     [_VP, ctypes.c_int, ctypes.c_int64, ctypes.c_char, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
     ("pjg_read_initial_conditions", ctypes.c_int,
      [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_char, _VP, _VP]),
     ("pjg_write_initial_conditions", ctypes.c_int,
@@ -96,6 +98,14 @@ SIGNATURES = [
 def launch_count():
     c = ctypes.c_int64()
     check("pjg_launch_count", load().pjg_launch_count(ctypes.byref(c)))
+    return c.value
+
+
+def eval_chunk(handle, kind, n, order, jac_format=0):
+    """States per launch of an evaluation of n states (pjg_eval_chunk)."""
+    c = ctypes.c_int64()
+    check("pjg_eval_chunk", load().pjg_eval_chunk(handle, int(kind), int(n), order.encode(),
+                                                  int(jac_format), ctypes.byref(c)))
     return c.value
 
 

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/pyjac_gb300.h"
+#include "../../include/pyjac_gb300_internal.h"
 #include "pjg_eval.cuh"
 #include "pjg_mlp.cuh"
 
@@ -194,7 +195,6 @@ int build_slots(pjg_mech* m, bool F, bool sparse, SlotTables** out)
         sp_slots[2 * k] = slot_of(m, F, sparse, 2 + k, 0);
         sp_slots[2 * k + 1] = slot_of(m, F, sparse, 2 + k, 1);
     }
-    row_off[last] = (int)row_list.size();
     for (int j = 0; j < last; ++j) {
         col_off[j] = (int)col_list.size();
         for (int k = 0; k < last; ++k) {
@@ -206,6 +206,7 @@ int build_slots(pjg_mech* m, bool F, bool sparse, SlotTables** out)
         if (cj_slots[2 * j] < 0 || cj_slots[2 * j + 1] < 0)
             return fail(PJG_ERR_TABLES, "Jacobian pattern lacks entries of rows T/E");
     }
+    row_off[last] = (int)row_list.size();
     col_off[last] = (int)col_list.size();
     t.s00 = slot_of(m, F, sparse, 0, 0);
     t.s01 = slot_of(m, F, sparse, 0, 1);
@@ -277,6 +278,19 @@ int ensure_work(pjg_mech* m, size_t bytes)
     return 0;
 }
 
+// The mechanism's tables live on the device that was current at
+// pjg_mech_create; a launch on another device would read them through
+// foreign addresses, so such calls are rejected.
+int check_device(const pjg_mech* m)
+{
+    int cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess) return fail(PJG_ERR_CUDA, "cudaGetDevice failed");
+    if (cur != m->device)
+        return fail(PJG_ERR_ARG, "mechanism was created on device %d, current device is %d",
+                    m->device, cur);
+    return 0;
+}
+
 void fill_common(const pjg_mech* m, EvalArgs& a)
 {
     memset(&a, 0, sizeof(a));
@@ -317,6 +331,7 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
     if (n == 0) return 0;
     if (!param || !phi || !out) return fail(PJG_ERR_ARG, "null array");
     if (kind == PJG_KIND_VJP && !v) return fail(PJG_ERR_ARG, "null vector");
+    if (int rc = check_device(m)) return rc;
     const bool F = order == 'F';
     const int NN = m->nn;
     SlotTables* t = nullptr;
@@ -405,8 +420,7 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
             cudaEventRecord(e0, st);
         }
         rc = pjg_launch_eval(a, kind, st);
-        if (rc) return fail(PJG_ERR_CUDA, "kernel launch failed: %s",
-                            cudaGetErrorString(cudaGetLastError()));
+        if (rc) return fail(PJG_ERR_CUDA, "kernel launch failed: %s", pjg_launch_error_string());
         g_launches.fetch_add(1);
         if (prof) {
             cudaEventRecord(e1, st);
@@ -429,6 +443,7 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
 int pjg_internal_fail(int code, const char* msg) { return fail(code, "%s", msg); }
 void pjg_internal_fill_args(const pjg_mech* m, EvalArgs* a) { fill_common(m, *a); }
 int pjg_internal_mech_ns(const pjg_mech* m) { return m->ns; }
+int pjg_internal_check_device(const pjg_mech* m) { return check_device(m); }
 void pjg_internal_count_launch() { g_launches.fetch_add(1); }
 
 extern "C" {
@@ -750,6 +765,23 @@ int pjg_jacobian_rates(pjg_mech* m, int64_t n, char order, int conp, int jac_for
                     nullptr, nullptr, 0, dphi);
 }
 
+int pjg_eval_chunk(pjg_mech* m, int kind, int64_t n, char order, int jac_format, int64_t* states)
+{
+    if (!states) return fail(PJG_ERR_ARG, "null argument");
+    if (kind < 0 || kind > 2) return fail(PJG_ERR_ARG, "bad kind");
+    *states = 0;
+    if (!m) return fail(PJG_ERR_ARG, "null mechanism");
+    if (order != 'C' && order != 'F') return fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
+    if (n <= 0) return 0;
+    SlotTables* t = nullptr;
+    if (kind == PJG_JACOBIAN) {
+        int rc = build_slots(m, order == 'F', jac_format == PJG_JAC_SPARSE, &t);
+        if (rc) return rc;
+    }
+    *states = chunk_states(eval_state_bytes(m, kind, order == 'F', t), n, wave_states(m, kind));
+    return 0;
+}
+
 int pjg_vjp(pjg_mech* m, int64_t n, char order, int conp, const double* param, const double* phi,
             const double* v, double* out, void* stream)
 {
@@ -958,12 +990,16 @@ int pjg_kernel_resize(pjg_kernel* k, size_t problem_size, size_t work_size)
     return 0;
 }
 
-int pjg_kernel_call(pjg_kernel* k, const double* param, const double* phi, double* out)
+}  // extern "C"
+
+namespace {
+
+// The copy-evaluate-copy pipeline of one pjg_kernel_call.  An error may return
+// with copies still queued on the kernel object's streams; the caller
+// synchronises them.
+int kernel_stream(pjg_kernel* k, const double* param, const double* phi, double* out)
 {
-    if (!k) return fail(PJG_ERR_ARG, "null kernel");
     const int64_t n = (int64_t)k->problem_size, nn = k->mech->nn, no = (int64_t)k->out_per_state;
-    if (n == 0) return 0;
-    if (!param || !phi || !out) return fail(PJG_ERR_ARG, "null array");
     const bool F = k->order == 'F';
     const int64_t C = k->chunk;
     for (int64_t c = 0, s0 = 0; s0 < n; ++c, s0 += C) {
@@ -983,10 +1019,7 @@ int pjg_kernel_call(pjg_kernel* k, const double* param, const double* phi, doubl
         if (c >= kRing) CUDA_TRY(cudaStreamWaitEvent(k->s_comp, k->ev_out[b], 0));
         int rc = run_eval(k->mech, k->kind, cnt, k->order, k->conp, k->jac_format, k->d_param[b],
                           k->d_phi[b], k->d_out[b], k->s_comp, nullptr, k->work, k->work_bytes);
-        if (rc) {
-            cudaStreamSynchronize(k->s_out);
-            return rc;
-        }
+        if (rc) return rc;
         CUDA_TRY(cudaEventRecord(k->ev_k[b], k->s_comp));
         CUDA_TRY(cudaStreamWaitEvent(k->s_out, k->ev_k[b], 0));
         if (F)
@@ -1000,6 +1033,26 @@ int pjg_kernel_call(pjg_kernel* k, const double* param, const double* phi, doubl
     CUDA_TRY(cudaStreamSynchronize(k->s_out));
     CUDA_TRY(cudaStreamSynchronize(k->s_comp));
     return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pjg_kernel_call(pjg_kernel* k, const double* param, const double* phi, double* out)
+{
+    if (!k) return fail(PJG_ERR_ARG, "null kernel");
+    if (k->problem_size == 0) return 0;
+    if (!param || !phi || !out) return fail(PJG_ERR_ARG, "null array");
+    const int rc = kernel_stream(k, param, phi, out);
+    if (rc) {
+        // copies from and to the caller's host arrays may still be queued: let
+        // them finish before the caller may free or reuse those arrays
+        cudaStreamSynchronize(k->s_in);
+        cudaStreamSynchronize(k->s_comp);
+        cudaStreamSynchronize(k->s_out);
+    }
+    return rc;
 }
 
 int pjg_kernel_required_memory(const pjg_kernel* k, size_t* bytes)

@@ -478,6 +478,12 @@ int pjg_eval_blocks_per_sm(int kind)
     return e == cudaSuccess && b > 0 ? b : 1;
 }
 
+namespace {
+thread_local cudaError_t g_launch_err = cudaSuccess;  // of this thread's last evaluation launch
+}
+
+const char* pjg_launch_error_string() { return cudaGetErrorString(g_launch_err); }
+
 int pjg_launch_eval(const EvalArgs& a, int kind, void* stream)
 {
     if (a.n <= 0) return 0;
@@ -486,5 +492,6 @@ int pjg_launch_eval(const EvalArgs& a, int kind, void* stream)
     if (kind == 1) launch<1>(a, grid, st);
     else if (kind == 2) launch<2>(a, grid, st);
     else launch<0>(a, grid, st);
-    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+    g_launch_err = cudaGetLastError();
+    return g_launch_err == cudaSuccess ? 0 : -2;
 }

@@ -63,6 +63,8 @@ struct EvalArgs {
 
 // host launchers (pjg_eval.cu)
 int pjg_launch_eval(const EvalArgs& a, int kind, void* stream);
+// CUDA's description of the error of this thread's last pjg_launch_eval
+const char* pjg_launch_error_string();
 // resident blocks per SM of the evaluation kernel of `kind`
 int pjg_eval_blocks_per_sm(int kind);
 int pjg_launch_zero(double* acc, int64_t ld, int64_t n, int nslot, void* stream);

@@ -42,6 +42,7 @@
 int pjg_internal_fail(int code, const char* msg);
 void pjg_internal_fill_args(const pjg_mech* m, EvalArgs* a);
 int pjg_internal_mech_ns(const pjg_mech* m);
+int pjg_internal_check_device(const pjg_mech* m);
 void pjg_internal_count_launch();
 
 namespace {
@@ -94,8 +95,12 @@ extern "C" int pjg_vjp_noalloc(pjg_mech* mech, int64_t n, char order, int conp, 
                  "the fixed %zu-byte array", ns, per_state * 8 * PJG_BLOCK, kScratchDoubles * 8);
         return pjg_internal_fail(PJG_ERR_ARG, msg);
     }
+    // the scratch address below is the current device's: the mechanism's
+    // tables must live there too
+    int rc = pjg_internal_check_device(mech);
+    if (rc) return rc;
     double* scratch = nullptr;
-    int rc = scratch_for_current_device(&scratch);
+    rc = scratch_for_current_device(&scratch);
     if (rc) return rc;
     if (chunk > n) chunk = n;
     const bool F = order == 'F';
@@ -123,7 +128,12 @@ extern "C" int pjg_vjp_noalloc(pjg_mech* mech, int64_t n, char order, int conp, 
         a.scratch = scratch;
         a.sc_ld = chunk;
         rc = pjg_launch_eval(a, 2, stream);
-        if (rc) return pjg_internal_fail(PJG_ERR_CUDA, "pjg_vjp_noalloc: kernel launch failed");
+        if (rc) {
+            char msg[256];
+            snprintf(msg, sizeof(msg), "pjg_vjp_noalloc: kernel launch failed: %s",
+                     pjg_launch_error_string());
+            return pjg_internal_fail(PJG_ERR_CUDA, msg);
+        }
         pjg_internal_count_launch();
     }
     return 0;
