@@ -43,43 +43,80 @@ __device__ __forceinline__ double mulpow(double acc, double v, int p)
     return acc * powi(v, p);
 }
 
-// Table of 2^(j/64), j = 0..63, in shared memory: every kernel that calls
-// fexp fills one per block with fill_exp_table before its first use.
-#define PJG_EXP_TAB 64
+// Table of 2^(j/2^B), j = 0 .. 2^B - 1, in shared memory (B = PJG_EXP_BITS):
+// every kernel that calls fexp fills one per block with fill_exp_table before
+// its first use.  B = 6 (64 entries) is the default.  Its random lookups meet
+// bank conflicts, which B = 4 (16 entries, one bank pair each) avoids and
+// B = 0 (no table) does without, both at the price of a longer polynomial.
+// Measured on GB300 (1,048,576 GRI-Mech 3.0 states, F order): the Jacobian
+// kernel takes 133 / 136.5 / 144 ms and the species-rate kernel 36.1 / 40.7 /
+// 47.0 ms for B = 6 / 4 / 0: the FP64 instruction count, not the shared-memory
+// lookups, sets the time.
+#ifndef PJG_EXP_BITS
+#define PJG_EXP_BITS 6
+#endif
+#define PJG_EXP_TAB (1 << PJG_EXP_BITS)
 
 __device__ __forceinline__ void fill_exp_table(double* tab)
 {
-    for (int j = threadIdx.x; j < PJG_EXP_TAB; j += blockDim.x) tab[j] = exp2((double)j * (1.0 / 64));
+    for (int j = threadIdx.x; j < PJG_EXP_TAB; j += blockDim.x)
+        tab[j] = exp2((double)j * (1.0 / PJG_EXP_TAB));
 }
 
 // exp(x) by the table-driven method of P. T. P. Tang ("Table-driven
 // implementation of the exponential function in IEEE floating-point
-// arithmetic", ACM TOMS 15(2), 1989): x = (64 m + j) ln2/64 + r with
-// |r| <= ln2/128, so exp(x) = 2^m 2^(j/64) exp(r), and exp(r) - 1 is its
-// degree-5 Taylor polynomial (truncation below 4e-17 relative).  Ten FP64
-// instructions; the scale 2^m goes into the exponent field with an integer
-// add.  |x| >= 708, infinities and NaN take the library exp.  Error about
-// 1 ulp (checked against exp in the tests).
+// arithmetic", ACM TOMS 15(2), 1989): x = (2^B m + j) ln2 / 2^B + r with
+// |r| <= ln2 / 2^(B+1), so exp(x) = 2^m 2^(j/2^B) exp(r), and exp(r) - 1 is
+// its Taylor polynomial, of degree 5 for B = 6 (|r| <= 0.0055, truncation
+// below 4e-17 relative), 7 for B = 4 (|r| <= 0.022, below 2e-18) and 13 for
+// B = 0 (|r| <= 0.35, below 5e-18).  The reduction is Cody and Waite's with
+// ln2 split in two (the leading part is the double nearest ln 2, the trailing
+// part the rest), each product taken by one FMA.  The scale 2^m goes into the
+// exponent field with an integer add.  |x| >= 708, infinities and NaN take
+// the library exp.  Tested against the CUDA library exp: within 3 ulp.
 __device__ __forceinline__ double fexp(double x, const double* tab)
 {
     if ((__double_as_longlong(x) & 0x7fffffffffffffffLL) >= 0x4086200000000000LL)  // |x| >= 708
         return exp(x);
-    const double inv = 92.33248261689366;          // 64 / ln 2
-    const double l1 = 0.010830424696249145;        // ln 2 / 64, leading part
-    const double l2 = 3.623510646634843e-19;       // ln 2 / 64 - l1
+    const double inv = 1.4426950408889634 * PJG_EXP_TAB;             // 2^B / ln 2
+    const double l1 = 0.6931471805599453 * (1.0 / PJG_EXP_TAB);       // ln 2 / 2^B, leading part
+    const double l2 = 2.3190468138462996e-17 * (1.0 / PJG_EXP_TAB);   // ln 2 / 2^B - l1
     const double shift = 6755399441055744.0;       // 1.5 * 2^52: rounds to an integer
     const double t = fma(x, inv, shift);
-    const double nd = t - shift;                   // nearest integer to 64 x / ln 2
+    const double nd = t - shift;                   // nearest integer to 2^B x / ln 2
     const int n = __double2loint(t);               // the same integer
     double r = fma(-nd, l1, x);
     r = fma(-nd, l2, r);
+    // q = (exp(r) - 1) / r by Horner's rule on the Taylor coefficients 1/k!
+#if PJG_EXP_BITS >= 6
     double q = fma(r, 1.0 / 120, 1.0 / 24);
+#elif PJG_EXP_BITS >= 4
+    double q = fma(r, 1.0 / 40320, 1.0 / 5040);
+    q = fma(q, r, 1.0 / 720);
+    q = fma(q, r, 1.0 / 120);
+    q = fma(q, r, 1.0 / 24);
+#else
+    double q = fma(r, 1.0 / 87178291200.0, 1.0 / 6227020800.0);
+    q = fma(q, r, 1.0 / 479001600.0);
+    q = fma(q, r, 1.0 / 39916800.0);
+    q = fma(q, r, 1.0 / 3628800.0);
+    q = fma(q, r, 1.0 / 362880.0);
+    q = fma(q, r, 1.0 / 40320);
+    q = fma(q, r, 1.0 / 5040);
+    q = fma(q, r, 1.0 / 720);
+    q = fma(q, r, 1.0 / 120);
+    q = fma(q, r, 1.0 / 24);
+#endif
     q = fma(q, r, 1.0 / 6);
     q = fma(q, r, 0.5);
     q = fma(q, r, 1.0);
+#if PJG_EXP_BITS > 0
     const double tj = tab[n & (PJG_EXP_TAB - 1)];
     const double y = fma(tj, r * q, tj);
-    return __longlong_as_double(__double_as_longlong(y) + ((long long)(n >> 6) << 52));
+#else
+    const double y = fma(r, q, 1.0);
+#endif
+    return __longlong_as_double(__double_as_longlong(y) + ((long long)(n >> PJG_EXP_BITS) << 52));
 }
 
 // exp(min(x, 690.775527898)), the reference's guarded exponential
