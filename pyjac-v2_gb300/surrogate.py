@@ -369,13 +369,43 @@ class Surrogate(object):
         out, lerr, X = self.predict(param, phi)
         return torch.cat([out[:, :1], out[:, 2:]], dim=1), lerr, X
 
+    def calibrate(self, n=1 << 18, seed=777, tols=(1.0, 0.5, 0.3, 1e-1, 1e-2, 1e-3),
+                  precision=0.99):
+        """Set the error head's threshold for each tolerance on held-out
+        states: the largest predicted log10 error tau such that, of the
+        held-out states whose prediction is at most tau, a fraction
+        `precision` is truly within the tolerance (the FP64 path judges).
+        Returns {tol: (tau, fraction of held-out states answered)}."""
+        data = self.make_data(n, seed=seed, sobolev=False)
+        y_hat, lerr, _ = self.predict_raw(data["P"], data["phi"])
+        err = torch.nan_to_num(self.rel_error(y_hat, data["y"]), nan=math.inf)
+        order = torch.argsort(lerr)
+        ls, es = lerr[order], err[order]
+        cnt = torch.arange(1, n + 1, device=ls.device, dtype=torch.float64)
+        self.thresholds = {}
+        rep = {}
+        for tol in tols:
+            ok = torch.cumsum((es <= tol).double(), 0) / cnt
+            good = torch.nonzero(ok >= precision).flatten()
+            # the longest prefix that keeps the precision, and at least 100 states
+            k = int(good.max()) + 1 if good.numel() and int(good.max()) >= 99 else 0
+            tau = float(ls[k - 1]) if k else -math.inf
+            self.thresholds[tol] = tau
+            rep[tol] = (tau, k / n)
+        self.calibration = {"states": n, "precision": precision, "thresholds": rep}
+        return rep
+
     def species_rates(self, param, phi, tol=1e-3, margin=0.5, return_info=False):
-        """dphi (n, NN) with the surrogate where trusted, FP64 elsewhere."""
+        """dphi (n, NN) with the surrogate where trusted, FP64 elsewhere.
+        Trusted: inside the training box and a predicted log10 error at most
+        the threshold calibrate() set for this tolerance (else log10(tol) -
+        margin)."""
         out, lerr, X = self.predict(param, phi)
         box_lo, box_hi = self.stats["box_lo"], self.stats["box_hi"]
         f = X[:, :2].float()
         ood = ((f < box_lo - 1e-3) | (f > box_hi + 1e-3)).any(dim=1)
-        fb = ood | (lerr > math.log10(tol) - margin) | ~torch.isfinite(out).all(dim=1)
+        tau = getattr(self, "thresholds", {}).get(tol, math.log10(tol) - margin)
+        fb = ood | (lerr > tau) | ~torch.isfinite(out).all(dim=1)
         idx = torch.nonzero(fb).flatten()
         if idx.numel():
             sub = self.ev.species_rates(param[idx].contiguous(), phi[idx].contiguous())

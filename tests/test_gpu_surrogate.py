@@ -72,31 +72,52 @@ def test_sobolev_training_and_fallback(cuda_device):
     assert s.eval_mse(data) < mse0
 
 
-def test_surrogate_inference_faster_than_fp64_kernel(cuda_device):
-    """What the network gains: its forward pass over 1M states against the FP64
-    species-rate kernel over the same states."""
+def test_trained_surrogate_with_fallback_beats_fp64_kernel(cuda_device):
+    """What the trained network gains over the method without it (the FP64
+    species-rate kernel alone): trained on the GPU by the tcgen05 kernels and
+    its error head calibrated on held-out states, the surrogate with per-state
+    FP64 fallback answers 1M fresh states faster than the FP64 kernel at the
+    tightest of the tolerances 1, 0.5, 0.3, 0.1 where it falls back for
+    fewer than half of them; an
+    untrained network of the same shape falls back for more states there.
+    Every state answered by the network meets the tolerance at the
+    calibrated rate or better, the FP64 kernel judging."""
     import torch
     sg = pkg("surrogate")
     mech = load_mech("gri30")
+    tols = (1.0, 0.5, 0.3, 0.1)
     s = sg.Surrogate(mech, device=cuda_device, seed=2)
-    s.make_data(1 << 14, seed=3, sobolev=False)  # fixes the normalisation
-    n = 1 << 20
-    P, phi = pkg("states").draw_states(mech.n_species, n, seed=4, x_floor=1e-12)
-    P = torch.from_numpy(P).to(cuda_device)
-    phi = torch.from_numpy(phi).to(cuda_device)
-    for _ in range(2):
-        s.predict_raw(P, phi)
-        s.ev.species_rates(P, phi)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    s.predict_raw(P, phi)
-    torch.cuda.synchronize()
-    t_net = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    s.ev.species_rates(P, phi)
-    torch.cuda.synchronize()
-    t_fp64 = time.perf_counter() - t0
-    assert t_net < t_fp64, (t_net, t_fp64)
+    s.fit(n_train=1 << 20, epochs=6, batch=16384, lr=2e-3)
+    s.calibrate(n=1 << 16, seed=31, tols=tols)
+    untrained = sg.Surrogate(mech, device=cuda_device, seed=2, evaluator=s.ev)
+    untrained.stats = s.stats
+    untrained.calibrate(n=1 << 16, seed=31, tols=tols)
+    data = s.make_data(1 << 20, seed=4, sobolev=False)
+    P, phi = data["P"], data["phi"]
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+
+    t_fp64, ref = timed(lambda: s.ev.species_rates(P, phi))
+    chosen = None
+    for tol in tols:  # loosest first: the last one kept is the tightest usable
+        _, (out, info) = timed(lambda: s.species_rates(P, phi, tol=tol, return_info=True))
+        if info["fallback_frac"] < 0.5:
+            chosen = tol
+    assert chosen is not None, "the trained network answers under half the states at every tolerance"
+    t_sur, (out, info) = timed(lambda: s.species_rates(P, phi, tol=chosen, return_info=True))
+    _, (_, info0) = timed(lambda: untrained.species_rates(P, phi, tol=chosen, return_info=True))
+    assert t_sur < t_fp64, (chosen, t_sur, t_fp64, info)
+    assert info0["fallback_frac"] > info["fallback_frac"], (chosen, info0, info)
+    # the answered states meet the tolerance (calibrated at 99 % on held-out data)
+    y = torch.cat([out[:, :1], out[:, 2:]], dim=1)
+    err = s.rel_error(y, data["y"])
+    assert float((err <= chosen).float().mean()) >= 0.97, (chosen, info)
 
 
 def test_fused_input_and_output_stages_match_torch(cuda_device):
