@@ -48,10 +48,10 @@ __device__ __forceinline__ double mulpow(double acc, double v, int p)
 // its first use.  B = 6 (64 entries) is the default.  Its random lookups meet
 // bank conflicts, which B = 4 (16 entries, one bank pair each) avoids and
 // B = 0 (no table) does without, both at the price of a longer polynomial.
-// Measured on GB300 (1,048,576 GRI-Mech 3.0 states, F order): the Jacobian
-// kernel takes 133 / 136.5 / 144 ms and the species-rate kernel 36.1 / 40.7 /
-// 47.0 ms for B = 6 / 4 / 0: the FP64 instruction count, not the shared-memory
-// lookups, sets the time.
+// Measured on GB300 (1,048,576 GRI-Mech 3.0 states, F order), B = 4 and
+// B = 0 against B = 6: the Jacobian kernel 2.6 % and 8.3 % slower, the
+// species-rate kernel 13 % and 30 % slower (40.7 and 47.0 ms against 36.1):
+// the FP64 instruction count, not the shared-memory lookups, sets the time.
 #ifndef PJG_EXP_BITS
 #define PJG_EXP_BITS 6
 #endif
