@@ -243,7 +243,10 @@ int pjg_write_initial_conditions(const char* filename, int64_t n, int32_t nn, ch
  * pjg_lu_factor_sparse: M_i = I - s h_i J_i as for pjg_lu_factor, factored
  * without interchanges in the permuted order: lu[i][r][c] (dense layout of
  * jac) holds the factors of M_i[perm[r]][perm[c]] (zeros outside the filled
- * pattern); info[i] = k for the first exactly zero pivot (1-based step).
+ * pattern); info[i] = k for the first exactly zero pivot (1-based step),
+ * -k when the first pivot that is not finite comes first (without
+ * interchanges a growing factor can overflow: the caller should then fall
+ * back to pjg_lu_factor), 0 otherwise.
  * pjg_lu_solve_sparse: b (laid out like phi, variables' order) <- M^-1 b.
  *
  * pjg_ros2_step: one step of the L-stable Rosenbrock method ROS2

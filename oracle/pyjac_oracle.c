@@ -1040,7 +1040,10 @@ int orc_lu_sparse_factor(int nn, long n, double s, const double* h, double h0, c
                 a[r * nn + c] = fma(-g, J[perm[r] * nn + perm[c]], r == c ? 1.0 : 0.0);
         for (int k = 0; k < nn; ++k) {
             const double p = a[k * nn + k];
-            if (p == 0.0 && !first_zero) first_zero = k + 1;
+            if (!first_zero) {
+                if (p == 0.0) first_zero = k + 1;
+                else if (!isfinite(p)) first_zero = -(k + 1);  /* overflow or NaN */
+            }
             if (roff[k + 1] == roff[k]) continue;
             if (p != 0.0)
                 for (int q = roff[k]; q < roff[k + 1]; ++q) {

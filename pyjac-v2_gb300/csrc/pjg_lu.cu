@@ -309,7 +309,14 @@ __global__ void __launch_bounds__(32 * S * kWarpsPerState) lu_sparse_kernel(long
         __syncthreads();
         for (int k = 0; k < nn; ++k) {
             const int r0 = proff[k], nr = proff[k + 1] - r0;
-            if (tid < S && smem[(size_t)tid * msz + k * pitch + k] == 0.0 && !fz[tid]) fz[tid] = k + 1;
+            if (tid < S && !fz[tid]) {
+                // first exactly zero pivot (k + 1), or first non-finite one, -(k + 1):
+                // without interchanges a growing factor overflows, which the
+                // caller learns from a negative info
+                const double pv = smem[(size_t)tid * msz + k * pitch + k];
+                if (pv == 0.0) fz[tid] = k + 1;
+                else if (!isfinite(pv)) fz[tid] = -(k + 1);
+            }
             if (nr == 0) continue;  // nothing below the pivot: no update, no barrier
             const int c0 = pcoff[k], nc = pcoff[k + 1] - c0;
             const int* R = pridx + r0;

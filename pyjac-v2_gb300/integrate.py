@@ -124,8 +124,10 @@ def lu_plan_info(evaluator):
 def lu_factor_sparse(evaluator, jac, h, s=1.0, order="C", out=None):
     """Static-pivot factorisation of M_i = I - s h_i J_i on the evaluator's
     mechanism plan.  Returns (lu, info): lu like jac, holding the factors of
-    the permuted matrix M[perm][:, perm]; info int32 (N,) = 0 or the 1-based
-    step of the first exactly zero pivot."""
+    the permuted matrix M[perm][:, perm]; info int32 (N,) = 0, the 1-based
+    step k of the first exactly zero pivot, or -k where a pivot that is not
+    finite comes first (overflow without interchanges: factor those states
+    with lu_factor instead)."""
     _check_f64(jac)
     n, nn = _n_of(jac, order)
     if nn != evaluator.nn:

@@ -278,7 +278,11 @@ class Surrogate(object):
 
     # ----------------------------------------------------------- training
     def fit(self, n_train=1 << 22, epochs=20, batch=16384, lr=2e-3, sobolev_weight=0.1,
-            delta=0.05, seed=0, log=None, err_head_from=0.3):
+            delta=0.05, seed=0, log=None, err_head_from=0.3, err_weight=0.1):
+        """Train on n_train fresh states: value MSE + sobolev_weight x the
+        directional-derivative MSE; from the fraction err_head_from of the
+        steps on, the error head regresses log10 of each state's current
+        relative error with weight err_weight."""
         data = self.make_data(n_train, seed)
         X, Tt, U, D = data["X"], data["T"], data["U"], data["D"]
         n = X.shape[0]
@@ -314,7 +318,7 @@ class Surrogate(object):
                         e = self.rel_error(yh, data["y"][idx])
                         e = torch.nan_to_num(e, nan=1e4, posinf=1e4).clamp(1e-8, 1e4)
                         tgt = torch.log10(e).float()
-                    dY[:batch, ERR] = 2.0 * (yb[:, ERR] - tgt) / batch * 0.1
+                    dY[:batch, ERR] = 2.0 * (yb[:, ERR] - tgt) / batch * err_weight
                 gW, gb = net.backward(xT, dY)
                 lr_t = lr * 0.5 * (1 + math.cos(math.pi * frac))
                 net.adam(gW, gb, lr_t)

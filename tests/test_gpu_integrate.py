@@ -227,19 +227,24 @@ def test_lu_factor_sparse_bitwise(cuda_device, order, name, per_state_h):
 
 def test_lu_factor_sparse_zero_pivot_info(cuda_device):
     """A state whose Newton matrix is exactly zero (s h = 1, J = I) reports
-    info = 1, as the oracle does."""
+    info = 1, and one whose second pivot overflows reports -2, as the oracle
+    does."""
     import torch
     orc = oracle_mod()
     integ = pkg("integrate")
     mech = load_mech("h2o2")
     plan = _plan(mech)
-    J = np.zeros((3, mech.nn, mech.nn))
+    J = np.zeros((4, mech.nn, mech.nn))
     J[1] = np.eye(mech.nn)
+    # state 3: the first elimination step overflows the second pivot
+    p0, p1 = plan["perm"][0], plan["perm"][1]
+    J[3][p1, p0] = J[3][p0, p1] = -1e200
     lu_ref, info_ref = orc.lu_factor_sparse(J, 1.0, 1.0, plan)
     ev = pkg("api").Evaluator(mech)
     lu, info = integ.lu_factor_sparse(ev, _to_dev_mat(J, "C", cuda_device), 1.0)
-    assert list(info.cpu().numpy()) == list(info_ref) == [0, 1, 0]
-    assert np.array_equal(lu.cpu().numpy(), lu_ref)
+    assert list(info.cpu().numpy()) == list(info_ref) == [0, 1, 0, -2]
+    bits = lambda a: np.ascontiguousarray(a).view(np.int64)
+    assert np.array_equal(bits(lu.cpu().numpy()), bits(lu_ref))
 
 
 @pytest.mark.parametrize("order", ["C", "F"])

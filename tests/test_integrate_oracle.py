@@ -226,3 +226,21 @@ def test_ros2_constant_volume_converges_at_second_order():
         errs.append((np.abs(y[0] - ref) / scale).max())
     rates = [errs[i] / errs[i + 1] for i in range(2)]
     assert all(3.0 < r < 5.5 for r in rates), (errs, rates)
+
+
+def test_sparse_lu_reports_overflowing_pivots():
+    """Without interchanges a pivot can overflow: info is then minus the
+    1-based step of the first non-finite pivot, and a zero pivot that comes
+    first keeps its positive step."""
+    orc = oracle_mod()
+    mech = load_mech("h2o2")
+    pk = pkg("pack").PackedTables(mech)
+    plan = orc.lu_plan(pk.crs_row_ptr, pk.crs_col_ind)
+    p0, p1, p2 = plan["perm"][:3]
+    J = np.zeros((3, mech.nn, mech.nn))
+    J[0][p1, p0] = J[0][p0, p1] = -1e200      # a_11 = 1 - 1e400: -inf at step 2
+    J[1][p2, p2] = 1.0                          # exactly zero pivot at step 3
+    J[2][p2, p2] = 1.0
+    J[2][p1, p0] = J[2][p0, p1] = -1e200      # the overflow (step 2) comes first
+    lu, info = orc.lu_factor_sparse(J, 1.0, 1.0, plan)
+    assert list(info) == [-2, 3, -2]
