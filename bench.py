@@ -331,11 +331,17 @@ def parity_check(mech, ev, kernel, fmt, order, P, phi, out, tP, tphi, tv=None, c
     dref = o.species_rates(Ps, phis, nthreads=thr)
     scale = o.rates_scale(Ps, phis, nthreads=thr)
     res["rates_max_rel"] = float((np.abs(dg - dref) / np.maximum(np.abs(dref), 1e-300)).max())
+    diff = np.abs(dg - dref)
     res["rates_max_rel_cancellation_scaled"] = float(
-        (np.abs(dg - dref) / np.maximum(np.maximum(np.abs(dref), scale * 1e-8), 1e-300)).max())
-    res["rates_bar"] = "1e-10 relative, entries below 1e-8 of their cancellation scale measured " \
-                       "against that scale"
-    res["rates_pass"] = bool(res["rates_max_rel_cancellation_scaled"] <= 1e-10)
+        (diff / np.maximum(np.abs(dref) + scale, 1e-300)).max())
+    well = np.abs(dref) >= 1e-3 * scale
+    res["rates_max_rel_well_conditioned"] = float((diff[well] / np.abs(dref[well])).max()) \
+        if well.any() else 0.0
+    res["rates_bar"] = "1e-10 relative to |value| + cancellation scale (the same sums in absolute " \
+                       "values) for every entry, and 1e-10 relative to |value| for entries of at " \
+                       "least 1e-3 of their scale"
+    res["rates_pass"] = bool(res["rates_max_rel_cancellation_scaled"] <= 1e-10 and
+                             res["rates_max_rel_well_conditioned"] <= 1e-10)
     if kernel == "vjp":
         got = gather_output(out, "vjp", fmt, order, n, nn, 0, idx)
         J = o.jacobian(Ps, phis, nthreads=thr)

@@ -55,7 +55,8 @@ def test_gpu_matches_shipped_reference_outputs(cuda_device, name):
     jac = ev.jacobian(tP, tphi, order="F", jac_format="sparse" if sparse else "full").cpu().numpy()
     dphi = ev.species_rates(tP, tphi, order="F").cpu().numpy()
     jr = g["jac_F"]
-    got = jac.reshape(jr.shape) if sparse else jac.reshape(NN, NN, n).transpose(1, 0, 2).reshape(NN * NN, n)
+    # both layouts index entry (row, col) of state s at (col * NN + row, s)
+    got = jac.reshape(jr.shape) if sparse else jac.reshape(NN * NN, n)
     Jg, _ = _dense_ref(got, mech)
     Jr, mask = _dense_ref(jr, mech)
     rowmax = np.abs(Jr).max(axis=2, keepdims=True)
@@ -66,12 +67,20 @@ def test_gpu_matches_shipped_reference_outputs(cuda_device, name):
     rel = err[well] / np.abs(Jr[well])
     assert well.sum() > 0.3 * n * mask.sum()
     assert float(rel.max()) <= 1e-8, float(rel.max())
-    # rates: relative to each entry, with entries below 1e-8 of their
-    # cancellation scale (the same sums in absolute values) measured against it
+    # rates, in two forms.  scale: the same sums in absolute values (the
+    # cancellation scale); an entry k times smaller than its scale carries
+    # about k * (number of terms) ulps of rounding in any FP64 evaluation, so
+    # a plain relative bar is asserted where k <= 1e3 and every entry is
+    # measured against |value| + scale
     scale = oracle_mod().Oracle(mech).rates_scale(P, phi).T
     dr = g["dphi_F"]
-    rr = np.abs(dphi - dr) / np.maximum(np.maximum(np.abs(dr), 1e-8 * scale), 1e-300)
-    assert float(rr.max()) <= 1e-10, float(rr.max())
+    diff = np.abs(dphi - dr)
+    rs = diff / np.maximum(np.abs(dr) + scale, 1e-300)
+    assert float(rs.max()) <= 1e-10, float(rs.max())
+    wellr = np.abs(dr) >= 1e-3 * scale
+    assert wellr.mean() > 0.5
+    rw = diff[wellr] / np.abs(dr[wellr])
+    assert float(rw.max()) <= 1e-10, float(rw.max())
 
 
 @pytest.mark.parametrize("conp", [True, False])
