@@ -334,7 +334,7 @@ def parity_check(mech, ev, kernel, fmt, order, P, phi, out, tP, tphi, tv=None, c
     diff = np.abs(dg - dref)
     res["rates_max_rel_cancellation_scaled"] = float(
         (diff / np.maximum(np.abs(dref) + scale, 1e-300)).max())
-    well = np.abs(dref) >= 1e-3 * scale
+    well = (np.abs(dref) >= 1e-3 * scale) & (dref != 0)
     res["rates_max_rel_well_conditioned"] = float((diff[well] / np.abs(dref[well])).max()) \
         if well.any() else 0.0
     res["rates_bar"] = "1e-10 relative to |value| + cancellation scale (the same sums in absolute " \
