@@ -70,6 +70,7 @@ ORC_CMP(!=)
 static inline orc_cd fmin(orc_cd a, orc_cd b) { ++g_c.minmax; return orc_cd(::fmin(a.v, b.v)); }
 static inline orc_cd fmax(orc_cd a, orc_cd b) { ++g_c.minmax; return orc_cd(::fmax(a.v, b.v)); }
 static inline orc_cd fabs(orc_cd a) { return orc_cd(::fabs(a.v)); }
+static inline bool isfinite(orc_cd a) { return std::isfinite(a.v); }
 static inline orc_cd fma(orc_cd a, orc_cd b, orc_cd c) { ++g_c.fma; return orc_cd(::fma(a.v, b.v, c.v)); }
 static inline orc_cd exp(orc_cd a) { ++g_c.exp; return orc_cd(::exp(a.v)); }
 static inline orc_cd log(orc_cd a) { ++g_c.log; return orc_cd(::log(a.v)); }
