@@ -602,6 +602,56 @@ def surrogate_bench(mech, ev, dev, n_train, epochs, n_eval, log=None, ablation=T
     return res
 
 
+STUDY_GRID = ((4, 12, 1 << 20), (4, 12, 1 << 22), (4, 30, 1 << 22), (4, 60, 1 << 22),
+              (4, 120, 1 << 22), (8, 30, 1 << 22), (2, 30, 1 << 22))
+
+
+def surrogate_study(mech, ev, dev, n_eval=1 << 20, grid=STUDY_GRID, log=None):
+    """Capacity study of the surrogate: for each (hidden layers, epochs,
+    training states) the per-state error on n_eval fresh states, the share of
+    states within 1e-1 / 1e-2 / 1e-3, and the same network evaluated with
+    FP32 weights and activations (plain torch, a measurement only), which
+    separates the BF16 rounding from the fit."""
+    import torch
+    sg = pkg("surrogate")
+    tols = (1e-1, 1e-2, 1e-3)
+    rows = []
+    for depth, epochs, n_train in grid:
+        s = sg.Surrogate(mech, device=dev, evaluator=ev, depth=depth)
+        t0 = time.time()
+        hist = s.fit(n_train=n_train, epochs=epochs, batch=16384, lr=2e-3, sobolev_weight=0.1)
+        torch.cuda.synchronize()
+        t_fit = time.time() - t0
+        data = s.make_data(n_eval, seed=4242, sobolev=False)
+        y_hat, _, X = s.predict_raw(data["P"], data["phi"])
+        err = s.rel_error(y_hat, data["y"])
+        with torch.no_grad():
+            a = X.float()
+            for l in range(depth):
+                a = torch.nn.functional.silu(a @ s.net.W[l].t() + s.net.b[l])
+            y32 = s.untransform((a @ s.net.W[-1].t() + s.net.b[-1])[:, :sg.NOUT])
+        err32 = s.rel_error(y32, data["y"])
+        q = torch.tensor([0.5, 0.9], device=err.device)
+        e, e32 = torch.quantile(err.float(), q), torch.quantile(err32.float(), q)
+        flops = 6.0 * 3 * n_train * epochs * sum(i * o for i, o in s.net.dims)
+        rows.append({"hidden_layers": depth, "width": sg.HID, "epochs": epochs,
+                     "train_states": n_train, "train_s": t_fit, "train_flops": flops,
+                     "final_value_mse": hist[-1]["value_mse"],
+                     "err_median": float(e[0]), "err_p90": float(e[1]),
+                     "frac_err_below": {str(t): float((err <= t).float().mean()) for t in tols},
+                     "fp32_err_median": float(e32[0]), "fp32_err_p90": float(e32[1]),
+                     "fp32_frac_err_below": {str(t): float((err32 <= t).float().mean())
+                                             for t in tols}})
+        if log:
+            log(rows[-1])
+        del s, data
+        torch.cuda.empty_cache()
+    return {"surrogate_study": rows, "eval_states": n_eval,
+            "error_metric": "per state ||(y_hat - y)/rms|| / ||y/rms|| over dT/dt and the 52 "
+                            "molar rates", "train_flops": "6 x 3 passes (value, +-delta "
+                            "directional) x states x epochs x sum of fan_in x fan_out"}
+
+
 def lu_flops_per_state(nn):
     """FP64 flops of one Newton-matrix factorisation: forming I - g J (one FMA
     per entry), scaling the columns (one multiply per subdiagonal entry) and
@@ -952,6 +1002,9 @@ def parse_args(argv=None):
     ap.add_argument("--sur-train", type=int, default=1 << 22)
     ap.add_argument("--sur-epochs", type=int, default=12)
     ap.add_argument("--sur-eval", type=int, default=1 << 22)
+    ap.add_argument("--surrogate-study", action="store_true",
+                    help="only the surrogate's capacity study (depth x epochs x training states); "
+                         "prints one JSON line")
     ap.add_argument("--jac-type", default="exact", choices=["exact", "approximate"],
                     help="Jacobian type: exact (headline) or the reference's approximate type, "
                          "without the bath-gas terms")
@@ -969,6 +1022,14 @@ def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         return run_reference(args)
+    if args.surrogate_study:
+        import torch
+        dev = torch.device("cuda:0")
+        mech = load_mech("gri30")
+        res = surrogate_study(mech, pkg("api").Evaluator(mech), dev,
+                              log=lambda r: print(json.dumps(r), file=sys.stderr, flush=True))
+        print(json.dumps(res))
+        return 0
     sh = pkg("shard")
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # not started by torchrun: one process per GPU, spawned here

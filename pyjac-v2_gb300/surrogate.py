@@ -35,12 +35,14 @@ FEAT_FLOOR = 1e-20  # concentration floor of the log features
 
 
 class MLP(object):
-    """Weights (FP32 master + BF16 copies) and the tcgen05 forward/backward."""
+    """Weights (FP32 master + BF16 copies) and the tcgen05 forward/backward.
+    depth: hidden layers of width HID (4 for the product network; the fused
+    single-launch inference is built for 4)."""
 
-    dims = [(NIN_P, HID), (HID, HID), (HID, HID), (HID, HID), (HID, NOUT_P)]
-
-    def __init__(self, device, seed=0):
+    def __init__(self, device, seed=0, depth=4):
         self.device = device
+        self.depth = int(depth)
+        self.dims = [(NIN_P, HID)] + [(HID, HID)] * (self.depth - 1) + [(HID, NOUT_P)]
         g = torch.Generator().manual_seed(seed)
         self.W, self.b = [], []
         for din, dout in self.dims:
@@ -63,7 +65,8 @@ class MLP(object):
     def refresh(self):
         self.Wb = [w.to(torch.bfloat16).contiguous() for w in self.W]
         self.Wtb = [w.t().contiguous().to(torch.bfloat16) for w in self.W]
-        self.Wp = [mlp_ops.pack_core(w) for w in self.Wb]  # operands of the fused forward
+        # operands of the fused forward (4 hidden layers only)
+        self.Wp = [mlp_ops.pack_core(w) for w in self.Wb] if self.depth == 4 else None
 
     def _get(self, key, shape, dtype):
         b = self._buf.get(key)
@@ -77,7 +80,7 @@ class MLP(object):
         M = X.shape[0]
         a = X
         self.saved = [] if keep else None
-        for l in range(4):
+        for l in range(self.depth):
             A = self._get(("A", l, keep), (M, HID), torch.bfloat16)
             Z = self._get(("Z", l), (M, HID), torch.bfloat16) if keep else None
             AT = self._get(("AT", l), (HID, M), torch.bfloat16) if keep else None
@@ -86,12 +89,15 @@ class MLP(object):
                 self.saved.append((Z, AT))
             a = A
         Y = out if out is not None else self._get(("Y", keep), (M, NOUT_P), torch.float32)
-        mlp_ops.linear(a, self.Wb[4], bias=self.b[4], Y32=Y)
+        mlp_ops.linear(a, self.Wb[-1], bias=self.b[-1], Y32=Y)
         return Y
 
     def infer(self, X, out=None):
         """Inference: the whole network in one fused tcgen05 launch (activations
-        stay on chip); same result as forward(X)."""
+        stay on chip); same result as forward(X).  Other depths run layer by
+        layer."""
+        if self.Wp is None:
+            return self.forward(X, out=out)
         return mlp_ops.forward_fused(X, self.Wp, self.b, Y=out)
 
     def backward(self, XT, dY):
@@ -99,10 +105,11 @@ class MLP(object):
         M = dY.shape[0]
         gW = [torch.zeros_like(w) for w in self.W]
         gb = [torch.zeros_like(b) for b in self.b]
-        gb[4] = dY.sum(0)
+        L = self.depth
+        gb[L] = dY.sum(0)
         dZ = dY.to(torch.bfloat16).contiguous()
         dZT = dZ.t().contiguous()
-        for l in range(4, -1, -1):
+        for l in range(L, -1, -1):
             inT = XT if l == 0 else self.saved[l - 1][1]
             mlp_ops.wgrad(dZT, inT, gW[l])
             if l > 0:
@@ -112,8 +119,8 @@ class MLP(object):
                 mlp_ops.linear(dZ, self.Wtb[l], zprev=Zp, Y=nd, YT=ndT, colsum=gb[l - 1])
                 dZ, dZT = nd, ndT
         gW[0] *= self.mask_in
-        gW[4] *= self.mask_out
-        gb[4][ERR + 1:] = 0.0
+        gW[L] *= self.mask_out
+        gb[L][ERR + 1:] = 0.0
         return gW, gb
 
     def adam(self, gW, gb, lr, b1=0.9, b2=0.999, eps=1e-8):
@@ -143,7 +150,7 @@ class MLP(object):
 class Surrogate(object):
     """The learned wdot surrogate of one mechanism (constant pressure, 'C' order)."""
 
-    def __init__(self, mech, device="cuda", seed=0, evaluator=None, target_scale=1.0):
+    def __init__(self, mech, device="cuda", seed=0, evaluator=None, target_scale=1.0, depth=4):
         """target_scale: the rates are mapped through asinh(y / (target_scale * rms));
         small values make the targets logarithmic, larger ones keep the
         dominant rates of a state closer to linear.  Measured on GRI-Mech 3.0
@@ -153,7 +160,7 @@ class Surrogate(object):
         self.target_scale = float(target_scale)
         self.device = torch.device(device)
         self.ev = evaluator if evaluator is not None else api.Evaluator(mech)
-        self.net = MLP(self.device, seed)
+        self.net = MLP(self.device, seed, depth)
         ns = mech.n_species
         if ns - 1 != NIN - 2:
             raise ValueError("the surrogate is sized for 53-species mechanisms (GRI-Mech 3.0)")
