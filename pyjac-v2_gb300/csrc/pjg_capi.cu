@@ -84,6 +84,7 @@ extern "C" int pjg_internal_lu_solve_sparse(const void* p, int64_t n, char order
 
 struct pjg_mech {
     int ns = 0, nr = 0, nn = 0, need_logP = 0, nnz = 0, jac_approx = 0;
+    int nr_e22 = 0;  // leading reactions of the class A + B <=> C + D
     int device = 0;
     PjgRxn* rxn = nullptr;
     double* sp = nullptr;
@@ -301,6 +302,7 @@ void fill_common(const pjg_mech* m, EvalArgs& a)
     a.aux = m->aux;
     a.ns = m->ns;
     a.nr = m->nr;
+    a.nr_e22 = m->nr_e22;
     a.need_logP = m->need_logP;
     a.jac_approx = m->jac_approx;
 }
@@ -633,6 +635,54 @@ int pjg_profile_end(int64_t* launches, double* total_ms)
     return rc;
 }
 
+namespace {
+
+// A reaction of the class A + B <=> C + D: four distinct species with unit
+// coefficients, reversible, an Arrhenius rate form, no third body, and
+// (P_atm / R)^nu_sum = 1 (nu_sum = 0).  241 of GRI-Mech 3.0's 325 reactions.
+bool is_e22(const PjgRxn& R)
+{
+    if (R.nspec != 4 || RX_FORM(R.flags) > FORM_ARR || !(R.flags & RX_REV) ||
+        RX_THD(R.flags) != THD_NONE || R.nu_sum != 0 || R.p[P_PSUM] != 1.0)
+        return false;
+    int nre = 0, npr = 0;
+    for (int e = 0; e < 4; ++e) {
+        const int f = ent_nuf(R.ent[e]), r = ent_nur(R.ent[e]);
+        if (f == 1 && r == 0) ++nre;
+        else if (f == 0 && r == 1) ++npr;
+        else return false;
+    }
+    return nre == 2 && npr == 2;
+}
+
+// Reactions of the class above go first, each with its entries reordered
+// reactants first (species order kept within each side), so that the kernels
+// evaluate them by straight-line code with coefficients known at compile
+// time; the others follow in mechanism order.  Nothing outside the kernels
+// depends on the reaction order: the species rates and the Jacobian are sums
+// over reactions, and the slot tables are built from these records.
+void order_reactions(pjg_mech* m)
+{
+    std::vector<PjgRxn> head, tail;
+    for (const PjgRxn& R : m->h_rxn) {
+        if (!is_e22(R)) {
+            tail.push_back(R);
+            continue;
+        }
+        PjgRxn c = R;
+        int q = 0;
+        for (int side = 0; side < 2; ++side)
+            for (int e = 0; e < 4; ++e)
+                if ((ent_nuf(R.ent[e]) == 1) == (side == 0)) c.ent[q++] = R.ent[e];
+        head.push_back(c);
+    }
+    m->nr_e22 = (int)head.size();
+    head.insert(head.end(), tail.begin(), tail.end());
+    m->h_rxn.swap(head);
+}
+
+}  // namespace
+
 int pjg_mech_create(const pjg_tables* tb, pjg_mech** out)
 {
     if (!tb || !out) return fail(PJG_ERR_ARG, "null argument");
@@ -674,6 +724,7 @@ int pjg_mech_create(const pjg_tables* tb, pjg_mech** out)
             delete m;
             return fail(PJG_ERR_TABLES, "third-body species out of range");
         }
+    order_reactions(m);
     m->crs_ptr.assign(tb->crs_row_ptr, tb->crs_row_ptr + NN + 1);
     m->crs_ind.assign(tb->crs_col_ind, tb->crs_col_ind + tb->nnz);
     m->ccs_ptr.assign(tb->ccs_col_ptr, tb->ccs_col_ptr + NN + 1);

@@ -170,8 +170,52 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         }
     }
 
-    // ---------------------------------------------------------------- reactions
-    for (int i = 0; i < a.nr; ++i) {
+    // ------------------------------------- reactions A + B <=> C + D (packed first)
+    for (int i = 0; i < a.nr_e22; ++i) {
+        E22Head h;
+        load_e22(a.rxn + i, h);
+        E22Terms o;
+        e22_terms<DER>(h, last, sv, conc, bk, db, o);
+        accum(wdot, h.s[0], -o.net);
+        accum(wdot, h.s[1], -o.net);
+        accum(wdot, h.s[2], o.net);
+        accum(wdot, h.s[3], o.net);
+        if (!DER) continue;
+        const bool hasns = (h.flags & RX_HASNS) && !a.jac_approx;
+        if (VJP) {
+            double w = 0.0;
+#pragma unroll
+            for (int ka = 0; ka < 4; ++ka)
+                if (h.s[ka] != last) w = ka < 2 ? w - hw[h.s[ka]] : w + hw[h.s[ka]];
+            if (w != 0.0) {
+#pragma unroll
+                for (int jb = 0; jb < 4; ++jb)
+                    if (h.s[jb] != last) accum(nsrow, h.s[jb], w * o.g[jb]);
+                if (hasns) vNS = fma(w, o.gns, vNS);
+                vout0 = fma(w, o.d0, vout0);
+                vout1 = fma(w, o.d1, vout1);
+            }
+            continue;
+        }
+        const int* slots = a.rxn_slots + __ldg(a.rxn_slot_off + i);
+        double* accs = a.acc + s;
+#pragma unroll
+        for (int ka = 0; ka < 4; ++ka) {
+            const int k = h.s[ka];
+            if (k == last) continue;
+            // row k gets -v (reactants) or +v (products); reductions as below
+#pragma unroll
+            for (int jb = 0; jb < 6; ++jb) {
+                const int sl = jb < 4 ? __ldg(slots + ka * 4 + jb) : __ldg(slots + 16 + 2 * ka + (jb - 4));
+                const double v = jb < 4 ? o.g[jb] : (jb == 4 ? o.d0 : o.d1);
+                if (sl >= 0) atomicAdd(accs + (int64_t)sl * a.acc_ld, ka < 2 ? -v : v);
+            }
+            if (hasns) accum(nsrow, k, ka < 2 ? -o.gns : o.gns);
+        }
+    }
+
+    // ------------------------------------------------------- other reactions
+    for (int i = a.nr_e22; i < a.nr; ++i) {
         RxnHead h;
         load_head(a.rxn + i, h);
         RxnTerms o;

@@ -29,6 +29,7 @@ struct EvalArgs {
     const double* thd_coef;
     const double* aux;
     int ns, nr;
+    int nr_e22;      // reactions [0, nr_e22) are of the class A + B <=> C + D (see pjg_rxn.cuh)
     int need_logP;
     int jac_approx;  // 'approximate' Jacobian type: no bath-gas terms in the species columns
     // states

@@ -346,4 +346,81 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
     o.d1 = d1;
 }
 
+// ------------------------------------------------------------------------
+// Reactions A + B <=> C + D (is_e22 in pjg_capi.cu: four distinct species
+// with unit coefficients, reversible, Arrhenius form, no third body,
+// nu_sum = 0), entries stored reactants first.  The same arithmetic as
+// rxn_terms() for this case with every stoichiometric branch resolved at
+// compile time: kr = kf exp(-sum nu b) (the (P_atm/R)^0 factor is 1),
+// d R / d c_j is one product per participant, and ci = 1.
+struct E22Head {
+    int flags, bint;
+    int s[4];  // reactant, reactant, product, product
+    const double* p;
+};
+
+__device__ __forceinline__ void load_e22(const PjgRxn* R, E22Head& h)
+{
+    const int4 h0 = __ldg(reinterpret_cast<const int4*>(R));
+    const int4 h1 = __ldg(reinterpret_cast<const int4*>(R) + 1);
+    const uint4 e0 = __ldg(reinterpret_cast<const uint4*>(R) + 2);
+    h.flags = h0.x;
+    h.bint = h1.z;
+    h.s[0] = ent_spec(e0.x);
+    h.s[1] = ent_spec(e0.y);
+    h.s[2] = ent_spec(e0.z);
+    h.s[3] = ent_spec(e0.w);
+    h.p = R->p;
+}
+
+struct E22Terms {
+    double net;   // rate of progress
+    double g[4];  // d net / d c_j of the four participants
+    double gns;   // the same for the bath gas (0 if it does not take part)
+    double d0, d1;
+};
+
+template <bool DER, class ARR>
+__device__ __forceinline__ void e22_terms(const E22Head& h, int last, const StateVars& sv,
+                                          const ARR& conc, const ARR& bk, const ARR& db,
+                                          E22Terms& o)
+{
+    const double* p = h.p;
+    const double b = ldg(p + P_B), Ta = ldg(p + P_TA);
+    const double kf = arrhenius(RX_FORM(h.flags), ldg(p + P_A), b, Ta, h.bint, sv.Tc, sv.logT,
+                                sv.Tinv, sv.etab);
+    double Bsum = 0.0 - bk[h.s[0]];
+    Bsum = Bsum - bk[h.s[1]];
+    Bsum = Bsum + bk[h.s[2]];
+    Bsum = Bsum + bk[h.s[3]];
+    const double kr = kf * fexp(-fmin(EXP_MAX, Bsum), sv.etab);
+    const double c0 = conc[h.s[0]], c1 = conc[h.s[1]], c2 = conc[h.s[2]], c3 = conc[h.s[3]];
+    const double rf = kf * c0 * c1, rr = kr * c2 * c3;
+    o.net = rf + -1.0 * rr;
+    if (!DER) return;
+    const double dlnkf_dT = (b + Ta * sv.Tjinv) * sv.Tjinv;
+    double dB = 0.0 - db[h.s[0]];
+    dB = dB - db[h.s[1]];
+    dB = dB + db[h.s[2]];
+    dB = dB + db[h.s[3]];
+    o.g[0] = kf * gsmall(c1);
+    o.g[1] = kf * gsmall(c0);
+    o.g[2] = -(kr * gsmall(c3));
+    o.g[3] = -(kr * gsmall(c2));
+    double gns = 0.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (h.s[j] == last) gns = o.g[j];
+    o.gns = gns;
+    const bool hasns = h.flags & RX_HASNS;
+    double d0 = rf * dlnkf_dT;
+    d0 = d0 + -1.0 * rr * (dlnkf_dT + -1.0 * dB);
+    d0 = d0 * sv.V;
+    if (hasns) d0 += -gns * sv.V * sv.PoRT * sv.Tjinv;
+    double d1 = sv.conp ? -rf + rr : 0.0;
+    if (hasns) d1 += gns * (sv.conp ? sv.PoRT : sv.V * sv.rt_inv);
+    o.d0 = d0;
+    o.d1 = d1;
+}
+
 }  // namespace pjg
