@@ -395,8 +395,11 @@ __device__ __forceinline__ void e22_terms(const E22Head& h, int last, const Stat
     Bsum = Bsum + bk[h.s[3]];
     const double kr = kf * fexp(-fmin(EXP_MAX, Bsum), sv.etab);
     const double c0 = conc[h.s[0]], c1 = conc[h.s[1]], c2 = conc[h.s[2]], c3 = conc[h.s[3]];
-    const double rf = kf * c0 * c1, rr = kr * c2 * c3;
-    o.net = rf + -1.0 * rr;
+    // rounded products and difference (no contraction into an FMA): the rate
+    // of progress must be the same in every kernel kind, whatever else uses
+    // rf and rr (the Jacobian's rates equal the rates kernel's bit for bit)
+    const double rf = __dmul_rn(__dmul_rn(kf, c0), c1), rr = __dmul_rn(__dmul_rn(kr, c2), c3);
+    o.net = __dsub_rn(rf, rr);
     if (!DER) return;
     const double dlnkf_dT = (b + Ta * sv.Tjinv) * sv.Tjinv;
     double dB = 0.0 - db[h.s[0]];
