@@ -747,6 +747,71 @@ def implicit_bench(mech, ev, dev, n, order, steps, warmup, fp64_peak):
     return res
 
 
+def implicit_large_bench(dev, n, fp64_peak, steps=2, warmup=1):
+    """The Newton-matrix factorisation beyond shared memory: the seeded
+    500-species synthetic mechanism (NN = 501), n states in C order, the dense
+    Jacobian factored by the blocked global-memory kernel, one solve, and one
+    whole ROS2 step (partial pivoting).  The oracle's operation count per
+    state (2/3 NN^3 + ...) sets the FP64 fraction."""
+    import torch
+    integ = pkg("integrate")
+    mech = load_mech("synthetic500")
+    ev = pkg("api").Evaluator(mech)
+    nn = mech.nn
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=2025, x_floor=1e-12)
+    tP = torch.from_numpy(P).to(dev)
+    tphi = torch.from_numpy(phi).to(dev)
+    h = torch.from_numpy(10.0 ** np.random.default_rng(6).uniform(-12, -9, n)).to(dev)
+    jac = ev.jacobian(tP, tphi, order="C")
+    lu = torch.empty_like(jac)
+    b = torch.randn(tphi.shape, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    piv = [None, None]
+
+    def factor():
+        _, piv[0], piv[1] = integ.lu_factor(jac, h, s=integ.ROS2_GAMMA, order="C", out=lu)
+
+    f_ms = timed(factor)
+    s_ms = timed(lambda: integ.lu_solve(lu, piv[0], b, order="C"))
+    singular = int((piv[1] != 0).sum())
+    del jac, lu
+    torch.cuda.empty_cache()
+    y, err = torch.empty_like(tphi), torch.empty_like(tphi)
+    st = integ.Ros2Stepper(ev, n, order="C")
+    r_ms = timed(lambda: st.step(tP, tphi, h, out=y, err=err))
+    fl = lu_flops_per_state(nn)
+    f_rate = n / (f_ms * 1e-3)
+    res = {"mechanism": "synthetic-500 (500 species, 2,500 reactions), NN = %d" % nn,
+           "states": n, "order": "C", "h": "per state, log-uniform 1e-12 .. 1e-9 s",
+           "factor": {"kernel": "lu_factor_big_kernel (one block per state, panels of 16 columns "
+                                "in shared memory, the matrix in global memory)",
+                      "ms": f_ms, "states_per_s": f_rate, "flops_per_state": fl,
+                      "fp64_tflops": fl * f_rate / 1e12, "fp64_frac": fl * f_rate / 1e12 / fp64_peak,
+                      "fp64_peak_source": "measured DFMA probe (pjg_fp64_peak)",
+                      "states_with_zero_pivot": singular},
+           "solve": {"kernel": "lu_solve_big_kernel (one thread per state, vector in place)",
+                     "ms": s_ms, "states_per_s": n / (s_ms * 1e-3),
+                     "hbm_gbs": (8 * nn * nn + 20 * nn) * n / (s_ms * 1e-3) / 1e9},
+           "ros2_step": {"ms": r_ms, "states_per_s": n / (r_ms * 1e-3),
+                         "path": "Ros2Stepper.step -> pjg_ros2_step (partial pivoting)"}}
+    del st, y, err
+    torch.cuda.empty_cache()
+    return res
+
+
 # ------------------------------------------------------------------ the line
 
 def headline_config(args, mech):
@@ -946,6 +1011,9 @@ def run_gpu(args):
     implicit = None
     if single and not args.no_implicit and args.kernel == "jacobian" and nn <= 169:
         implicit = implicit_bench(mech, ev, dev, n, args.order, args.steps, args.warmup, fp64_peak)
+        if args.mech == "gri30" and args.format == "full" and args.jac_type == "exact" and \
+                args.implicit_large_states > 0:
+            implicit["synthetic500"] = implicit_large_bench(dev, args.implicit_large_states, fp64_peak)
 
     configs = None
     if single and not args.no_configs and args.mech == "gri30" and args.kernel == "jacobian" \
@@ -999,6 +1067,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-implicit", action="store_true",
                     help="skip the implicit-step block (Newton-matrix LU, solve, ROS2 step)")
+    ap.add_argument("--implicit-large-states", type=int, default=4096,
+                    help="states of the synthetic-500 Newton-matrix block (0: skip it)")
     ap.add_argument("--sur-train", type=int, default=1 << 22)
     ap.add_argument("--sur-epochs", type=int, default=12)
     ap.add_argument("--sur-eval", type=int, default=1 << 22)

@@ -226,8 +226,10 @@ int pjg_write_initial_conditions(const char* filename, int64_t n, int32_t nn, ch
  * diagonal, not stored) below and U on and above the diagonal.  piv: nn
  * 1-based row interchanges per state, laid out like phi; info[n] (optional):
  * 0, or k for the first exactly zero pivot U(k,k) (1-based; LAPACK's info).
- * 1 <= nn <= 169 (the matrix of one state lives in shared memory);
- * larger mechanisms return PJG_ERR_UNSUPPORTED.
+ * 1 <= nn <= 4096: up to 169 a state's matrix lives in shared memory; above,
+ * it is factored in place in lu (global memory) in panels of up to 16
+ * columns, with the same operations in the same order, so the factors are
+ * the same; larger sizes return PJG_ERR_UNSUPPORTED.
  * pjg_lu_solve: b (laid out like phi) <- M^-1 b from pjg_lu_factor's output.
  *
  * Static-pivot sparse LU (the factorisation of implicit chemistry solvers
@@ -238,7 +240,7 @@ int pjg_write_initial_conditions(const char* filename, int64_t n, int32_t nn, ch
  * symbolically; step k then updates only the filled pattern's rows x
  * columns.  pjg_lu_symbolic: that order and the counts (FMAs per state,
  * entries of L + U) for a CRS pattern, host only, any nn up to 4,096 (to
- * size larger mechanisms' factorisations; the kernels take nn <= 169).  pjg_lu_plan_info: the same
+ * size larger mechanisms' factorisations; the sparse kernels take nn <= 169).  pjg_lu_plan_info: the same
  * for a mechanism (the plan is built on first use and kept with it).
  * pjg_lu_factor_sparse: M_i = I - s h_i J_i as for pjg_lu_factor, factored
  * without interchanges in the permuted order: lu[i][r][c] (dense layout of

@@ -921,8 +921,11 @@ int orc_chem_utils(const orc_mech* m, long n, int conp, const double* phi, doubl
  * operation order of the CUDA kernels so that results agree bit for bit:
  * entries fma(-s h_i, J, delta), pivot = first largest |a| in the column,
  * whole-row interchange, scale by 1/pivot (or divide below DBL_MIN), rank-1
- * update a_rc = fma(-l_r, u_c, a_rc); solves accumulate each row's dot product
- * in increasing column order by FMA and divide by U's diagonal). */
+ * update a_rc = fma(-l_r, u_c, a_rc); solves in the column order of LAPACK's
+ * dtrsv on a column-major matrix: the unit-lower pass subtracts each solved
+ * y_c from the rows below in increasing c, the upper pass divides y_c by U's
+ * diagonal and subtracts it from the rows above in decreasing c, each row
+ * accumulating by FMA). */
 int orc_lu_factor(int nn, long n, double s, const double* h, double h0, const double* jac,
                   double* lu, int* piv, int* info)
 {
@@ -983,15 +986,11 @@ int orc_lu_solve(int nn, long n, const double* lu, const int* piv, double* b)
                 y[p] = t;
             }
         }
-        for (int r = 1; r < nn; ++r) {
-            double acc = y[r];
-            for (int c = 0; c < r; ++c) acc = fma(-a[r * nn + c], y[c], acc);
-            y[r] = acc;
-        }
-        for (int r = nn - 1; r >= 0; --r) {
-            double acc = y[r];
-            for (int c = r + 1; c < nn; ++c) acc = fma(-a[r * nn + c], y[c], acc);
-            y[r] = acc / a[r * nn + r];
+        for (int c = 0; c < nn; ++c)
+            for (int r = c + 1; r < nn; ++r) y[r] = fma(-a[r * nn + c], y[c], y[r]);
+        for (int c = nn - 1; c >= 0; --c) {
+            y[c] = y[c] / a[c * nn + c];
+            for (int r = 0; r < c; ++r) y[r] = fma(-a[r * nn + c], y[c], y[r]);
         }
     }
     return 0;

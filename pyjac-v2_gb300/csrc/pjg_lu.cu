@@ -398,8 +398,10 @@ __global__ void __launch_bounds__(128) lu_sparse_solve_kernel(long long n, const
 }
 
 // one thread per state: row interchanges, unit-lower then upper substitution
-// (row-oriented: each y_r accumulates its dot product in increasing column
-// order by FMA, and the upper rows divide by the diagonal)
+// in the column order of LAPACK's dtrsv on a column-major matrix (the lower
+// pass subtracts each y_c from the rows below in increasing c; the upper pass
+// divides y_c by the diagonal and subtracts it from the rows above in
+// decreasing c; every row accumulates by FMA)
 template <bool F>
 __global__ void __launch_bounds__(128) lu_solve_kernel(int nn, long long n,
                                                        const double* __restrict__ lu,
@@ -418,6 +420,9 @@ __global__ void __launch_bounds__(128) lu_solve_kernel(int nn, long long n,
             y[p] = t;
         }
     }
+    // row by row with a register accumulator: each row takes the same FMAs in
+    // the same order as in the column sweeps (lower: c increasing; upper: c
+    // decreasing from nn - 1)
     for (int r = 1; r < nn; ++r) {
         double acc = y[r];
         for (int c = 0; c < r; ++c) acc = fma(-__ldg(lu + mat_idx(F, i, n, nn, r, c)), y[c], acc);
@@ -425,10 +430,273 @@ __global__ void __launch_bounds__(128) lu_solve_kernel(int nn, long long n,
     }
     for (int r = nn - 1; r >= 0; --r) {
         double acc = y[r];
-        for (int c = r + 1; c < nn; ++c) acc = fma(-__ldg(lu + mat_idx(F, i, n, nn, r, c)), y[c], acc);
+        for (int c = nn - 1; c > r; --c) acc = fma(-__ldg(lu + mat_idx(F, i, n, nn, r, c)), y[c], acc);
         y[r] = acc / __ldg(lu + mat_idx(F, i, n, nn, r, r));
     }
     for (int r = 0; r < nn; ++r) b[vec_idx(F, i, n, nn, r)] = y[r];
+}
+
+// ---- Newton matrices too large for shared memory (nn > 169, up to 4096):
+// one block of 256 threads per state, the matrix in global memory (the
+// output array, factored in place), a blocked right-looking LU with panels of
+// NB columns held in shared memory.  For each panel:
+//   1. the panel (rows k0.., columns k0..k0+NB-1) is factored in shared
+//      memory by the unblocked steps of lu_factor_kernel: pivot (first
+//      largest |a|, bit-pattern comparison), whole-row interchange within the
+//      panel, multipliers by the reciprocal, rank-1 update of the panel;
+//   2. each thread owns whole columns outside the panel: it applies the
+//      panel's interchanges to them in order, and for a column right of the
+//      panel forms U's NB entries by forward substitution with the panel's
+//      unit-lower block, then updates the column below by the NB multipliers.
+// Every entry receives the same FMAs in the same order (k = 0, 1, ...) as in
+// the unblocked algorithm, so the factors equal lu_factor_kernel's and the
+// oracle's bit for bit; blocking only cuts the passes over the trailing
+// matrix from nn to nn / NB.
+constexpr int kBigThreads = 256;
+constexpr int kBigMaxNN = 4096;
+
+template <bool F, int NB>
+__global__ void __launch_bounds__(kBigThreads, 2) lu_factor_big_kernel(int nn, long long n, double s,
+                                                                    const double* __restrict__ h,
+                                                                    double h0, const double* jac,
+                                                                    double* lu, int32_t* __restrict__ piv,
+                                                                    int32_t* __restrict__ info)
+{
+    extern __shared__ double P[];  // panel, column-major: P[cc * nn + rr], rr < nn - k0
+    __shared__ long long wbest[kBigThreads / 32];
+    __shared__ int wrow[kBigThreads / 32];
+    __shared__ int spiv[NB];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = kBigThreads / 32;
+    for (long long i = blockIdx.x; i < n; i += gridDim.x) {
+        auto A = [&](int r, int c) -> double& { return lu[mat_idx(F, i, n, nn, r, c)]; };
+        const double g = s * (h ? h[i] : h0);
+        const long long nsq = (long long)nn * nn;
+        for (long long e = tid; e < nsq; e += kBigThreads) {
+            // C order: consecutive threads along a row; F order: down a column
+            const int r = F ? (int)(e % nn) : (int)(e / nn), c = F ? (int)(e / nn) : (int)(e % nn);
+            const size_t o = mat_idx(F, i, n, nn, r, c);
+            lu[o] = fma(-g, jac[o], r == c ? 1.0 : 0.0);  // in place when lu == jac
+        }
+        __syncthreads();
+        int first_zero = 0;
+        for (int k0 = 0; k0 < nn; k0 += NB) {
+            const int w = nn - k0 < NB ? nn - k0 : NB, m = nn - k0;
+            for (int e = tid; e < m * w; e += kBigThreads) {
+                const int cc = e / m, rr = e - cc * m;
+                P[cc * m + rr] = A(k0 + rr, k0 + cc);
+            }
+            __syncthreads();
+            for (int kk = 0; kk < w; ++kk) {
+                double* col = P + kk * m;
+                long long best = -1;
+                int br = kk;
+                for (int rr = kk + tid; rr < m; rr += kBigThreads) {
+                    const long long v = __double_as_longlong(col[rr]) & kAbsMask;
+                    if (v > best) {
+                        best = v;
+                        br = rr;
+                    }
+                }
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+                    const int orr = __shfl_xor_sync(0xffffffffu, br, off);
+                    if (ob > best || (ob == best && orr < br)) {
+                        best = ob;
+                        br = orr;
+                    }
+                }
+                if (lane == 0) {
+                    wbest[warp] = best;
+                    wrow[warp] = br;
+                }
+                __syncthreads();
+                best = wbest[0];
+                br = wrow[0];
+#pragma unroll
+                for (int q = 1; q < NW; ++q)
+                    if (wbest[q] > best || (wbest[q] == best && wrow[q] < br)) {
+                        best = wbest[q];
+                        br = wrow[q];
+                    }
+                const bool nonzero = best > 0;
+                if (tid == 0) {
+                    spiv[kk] = nonzero ? br : kk;
+                    piv[vec_idx(F, i, n, nn, k0 + kk)] = k0 + (nonzero ? br : kk) + 1;
+                    if (!nonzero && !first_zero) first_zero = k0 + kk + 1;
+                }
+                if (nonzero && br != kk)  // whole rows of the panel
+                    for (int cc = tid; cc < w; cc += kBigThreads) {
+                        double* pc = P + cc * m;
+                        const double t = pc[kk];
+                        pc[kk] = pc[br];
+                        pc[br] = t;
+                    }
+                __syncthreads();
+                if (nonzero) {
+                    const double p = col[kk];
+                    if (best >= kDblMinBits) {
+                        const double inv = __drcp_rn(p);
+                        for (int rr = kk + 1 + tid; rr < m; rr += kBigThreads) col[rr] *= inv;
+                    } else {
+                        for (int rr = kk + 1 + tid; rr < m; rr += kBigThreads) col[rr] /= p;
+                    }
+                }
+                __syncthreads();
+                // rank-1 update of the panel's columns right of kk
+                const int mr = m - kk - 1, nc = w - kk - 1;
+                for (int e = tid; e < mr * nc; e += kBigThreads) {
+                    const int cq = e / mr, rq = e - cq * mr;
+                    const int cc = kk + 1 + cq, rr = kk + 1 + rq;
+                    P[cc * m + rr] = fma(-col[rr], P[cc * m + kk], P[cc * m + rr]);
+                }
+                __syncthreads();
+            }
+            for (int e = tid; e < m * w; e += kBigThreads) {
+                const int cc = e / m, rr = e - cc * m;
+                A(k0 + rr, k0 + cc) = P[cc * m + rr];
+            }
+            // columns outside the panel, one thread each
+            for (int c = tid; c < nn - w; c += kBigThreads) {
+                const int cg = c < k0 ? c : c + w;
+#pragma unroll 1
+                for (int kk = 0; kk < w; ++kk) {
+                    const int br = spiv[kk];
+                    if (br != kk) {
+                        double& x = A(k0 + kk, cg);
+                        double& y = A(k0 + br, cg);
+                        const double t = x;
+                        x = y;
+                        y = t;
+                    }
+                }
+                if (cg < k0) continue;
+                double u[NB];
+#pragma unroll
+                for (int q = 0; q < NB; ++q)
+                    if (q < w) u[q] = A(k0 + q, cg);
+#pragma unroll
+                for (int q = 1; q < NB; ++q)
+                    if (q < w)
+#pragma unroll
+                        for (int t = 0; t < NB; ++t)
+                            if (t < q) u[q] = fma(-P[t * m + q], u[t], u[q]);
+#pragma unroll
+                for (int q = 1; q < NB; ++q)
+                    if (q < w) A(k0 + q, cg) = u[q];
+                // rows below the panel, four at a time (independent FMA chains)
+                int r = w;
+                for (; r + 4 <= m; r += 4) {
+                    double a0 = A(k0 + r, cg), a1 = A(k0 + r + 1, cg), a2 = A(k0 + r + 2, cg),
+                           a3 = A(k0 + r + 3, cg);
+#pragma unroll
+                    for (int q = 0; q < NB; ++q)
+                        if (q < w) {
+                            const double* Lq = P + q * m + r;
+                            a0 = fma(-Lq[0], u[q], a0);
+                            a1 = fma(-Lq[1], u[q], a1);
+                            a2 = fma(-Lq[2], u[q], a2);
+                            a3 = fma(-Lq[3], u[q], a3);
+                        }
+                    A(k0 + r, cg) = a0;
+                    A(k0 + r + 1, cg) = a1;
+                    A(k0 + r + 2, cg) = a2;
+                    A(k0 + r + 3, cg) = a3;
+                }
+                for (; r < m; ++r) {
+                    double a0 = A(k0 + r, cg);
+#pragma unroll
+                    for (int q = 0; q < NB; ++q)
+                        if (q < w) a0 = fma(-P[q * m + r], u[q], a0);
+                    A(k0 + r, cg) = a0;
+                }
+            }
+            __syncthreads();
+        }
+        if (tid == 0 && info) info[i] = first_zero;
+        __syncthreads();
+    }
+}
+
+// The solve of lu_solve_kernel for nn > 176, one block of kSolveThreads per
+// state (the column order lets the rows of one step proceed in parallel):
+// the vector in shared memory, thread t owning rows t, t + T, ...; a barrier
+// between column steps; each step's factor entries loaded one step ahead.
+// Same operations in the same order as lu_solve_kernel and the oracle.
+constexpr int kSolveThreads = 128;
+
+template <bool F, int kSolveRows>  // rows per thread: kSolveRows * kSolveThreads >= nn
+__global__ void __launch_bounds__(kSolveThreads) lu_solve_big_kernel(int nn, long long n,
+                                                                     const double* __restrict__ lu,
+                                                                     const int32_t* __restrict__ piv,
+                                                                     double* b)
+{
+    extern __shared__ double y[];  // nn: accumulators; then nn: solved values
+    double* x = y + nn;
+    const int tid = threadIdx.x;
+    for (long long i = blockIdx.x; i < n; i += gridDim.x) {
+        for (int r = tid; r < nn; r += kSolveThreads) y[r] = b[vec_idx(F, i, n, nn, r)];
+        __syncthreads();
+        if (tid == 0)
+            for (int k = 0; k < nn; ++k) {
+                const int p = piv[vec_idx(F, i, n, nn, k)] - 1;
+                if (p > k && p < nn) {
+                    const double t = y[k];
+                    y[k] = y[p];
+                    y[p] = t;
+                }
+            }
+        __syncthreads();
+        // unit lower: step c subtracts y_c from rows r > c
+        double nxt[kSolveRows];
+#pragma unroll
+        for (int q = 0; q < kSolveRows; ++q) {
+            const int r = tid + q * kSolveThreads;
+            nxt[q] = r > 0 && r < nn ? __ldg(lu + mat_idx(F, i, n, nn, r, 0)) : 0.0;
+        }
+        for (int c = 0; c < nn - 1; ++c) {
+            double cur[kSolveRows];
+#pragma unroll
+            for (int q = 0; q < kSolveRows; ++q) {
+                cur[q] = nxt[q];
+                const int r = tid + q * kSolveThreads;
+                nxt[q] = r > c + 1 && r < nn ? __ldg(lu + mat_idx(F, i, n, nn, r, c + 1)) : 0.0;
+            }
+            const double yc = y[c];  // final: rows <= c take no more updates
+#pragma unroll
+            for (int q = 0; q < kSolveRows; ++q) {
+                const int r = tid + q * kSolveThreads;
+                if (r > c && r < nn) y[r] = fma(-cur[q], yc, y[r]);
+            }
+            __syncthreads();
+        }
+        // upper: step c divides y_c by the diagonal, subtracts it from rows r < c
+#pragma unroll
+        for (int q = 0; q < kSolveRows; ++q) {
+            const int r = tid + q * kSolveThreads;
+            nxt[q] = r < nn - 1 ? __ldg(lu + mat_idx(F, i, n, nn, r, nn - 1)) : 0.0;
+        }
+        for (int c = nn - 1; c >= 0; --c) {
+            double cur[kSolveRows];
+#pragma unroll
+            for (int q = 0; q < kSolveRows; ++q) {
+                cur[q] = nxt[q];
+                const int r = tid + q * kSolveThreads;
+                nxt[q] = c > 0 && r < c - 1 ? __ldg(lu + mat_idx(F, i, n, nn, r, c - 1)) : 0.0;
+            }
+            const double yc = y[c] / __ldg(lu + mat_idx(F, i, n, nn, c, c));
+            if (tid == c % kSolveThreads) x[c] = yc;
+#pragma unroll
+            for (int q = 0; q < kSolveRows; ++q) {
+                const int r = tid + q * kSolveThreads;
+                if (r < c) y[r] = fma(-cur[q], yc, y[r]);
+            }
+            __syncthreads();
+        }
+        for (int r = tid; r < nn; r += kSolveThreads) b[vec_idx(F, i, n, nn, r)] = x[r];
+        __syncthreads();
+    }
 }
 
 // Stage arithmetic of the two-stage Rosenbrock method ROS2, element-wise with
@@ -479,6 +747,48 @@ int lu_factor_launch(int nn, long long n, char order, double s, const double* h,
         lu_factor_kernel<true, S><<<(int)grid, threads, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
     else
         lu_factor_kernel<false, S><<<(int)grid, threads, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
+    return 0;
+}
+
+template <int NB>
+int lu_factor_big_launch(int nn, long long n, char order, double s, const double* h, double h0,
+                         const double* jac, double* lu, int32_t* piv, int32_t* info, cudaStream_t st,
+                         int sms)
+{
+    const size_t smem = (size_t)nn * NB * sizeof(double);
+    const void* fn = (const void*)lu_factor_big_kernel<false, NB>;
+    const void* fnF = (const void*)lu_factor_big_kernel<true, NB>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(fnF, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return pjg_internal_fail(PJG_ERR_CUDA, "cannot reserve shared memory for the LU kernel");
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBigThreads, smem) != cudaSuccess ||
+        per_sm < 1)
+        return pjg_internal_fail(PJG_ERR_CUDA, "LU kernel does not fit on the device");
+    long long grid = (long long)sms * per_sm;
+    if (n < grid) grid = n;
+    if (order == 'F')
+        lu_factor_big_kernel<true, NB><<<(int)grid, kBigThreads, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
+    else
+        lu_factor_big_kernel<false, NB><<<(int)grid, kBigThreads, smem, st>>>(nn, n, s, h, h0, jac, lu, piv, info);
+    return 0;
+}
+
+template <int R>
+int lu_solve_big_launch(int nn, long long n, char order, const double* lu, const int32_t* piv,
+                        double* b, cudaStream_t st)
+{
+    const size_t smem = 2 * (size_t)nn * sizeof(double);
+    const void* fn = (const void*)lu_solve_big_kernel<false, R>;
+    const void* fnF = (const void*)lu_solve_big_kernel<true, R>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(fnF, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return pjg_internal_fail(PJG_ERR_CUDA, "cannot reserve shared memory for the LU solve");
+    const int grid = (int)(n < (1 << 30) ? n : (1 << 30));
+    if (order == 'F')
+        lu_solve_big_kernel<true, R><<<grid, kSolveThreads, smem, st>>>(nn, n, lu, piv, b);
+    else
+        lu_solve_big_kernel<false, R><<<grid, kSolveThreads, smem, st>>>(nn, n, lu, piv, b);
     return 0;
 }
 
@@ -625,7 +935,7 @@ extern "C" int pjg_internal_lu_factor(int32_t nn, int64_t n, char order, double 
                            const double* jac, double* lu, int32_t* piv, int32_t* info,
                            cudaStream_t st)
 {
-    if (nn < 1 || nn > kLuMaxNN) return pjg_internal_fail(PJG_ERR_UNSUPPORTED, "LU: nn must be in [1, 169]");
+    if (nn < 1 || nn > kBigMaxNN) return pjg_internal_fail(PJG_ERR_UNSUPPORTED, "LU: nn must be in [1, 4096]");
     if (n < 0) return pjg_internal_fail(PJG_ERR_ARG, "negative problem size");
     if (order != 'C' && order != 'F') return pjg_internal_fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
     if (n == 0) return 0;
@@ -634,7 +944,15 @@ extern "C" int pjg_internal_lu_factor(int32_t nn, int64_t n, char order, double 
     if (int rc = sm_count(&sms)) return rc;
     const size_t per_state = (size_t)nn * (nn | 1) * sizeof(double) + (size_t)nn * sizeof(int);
     int rc;
-    if (kLuMaxStates * per_state <= kSmemLimit)
+    if (nn > kLuMaxNN) {
+        // global-memory blocked factorisation; panel width by the shared memory it takes
+        if ((size_t)nn * 16 * sizeof(double) <= kSmemLimit)
+            rc = lu_factor_big_launch<16>(nn, n, order, s, h, h0, jac, lu, piv, info, st, sms);
+        else if ((size_t)nn * 8 * sizeof(double) <= kSmemLimit)
+            rc = lu_factor_big_launch<8>(nn, n, order, s, h, h0, jac, lu, piv, info, st, sms);
+        else
+            rc = lu_factor_big_launch<4>(nn, n, order, s, h, h0, jac, lu, piv, info, st, sms);
+    } else if (kLuMaxStates * per_state <= kSmemLimit)
         rc = lu_factor_launch<kLuMaxStates>(nn, n, order, s, h, h0, jac, lu, piv, info, st, sms);
     else if (2 * per_state <= kSmemLimit)
         rc = lu_factor_launch<2>(nn, n, order, s, h, h0, jac, lu, piv, info, st, sms);
@@ -649,13 +967,20 @@ extern "C" int pjg_internal_lu_factor(int32_t nn, int64_t n, char order, double 
 extern "C" int pjg_internal_lu_solve(int32_t nn, int64_t n, char order, const double* lu, const int32_t* piv,
                           double* b, cudaStream_t st)
 {
-    if (nn < 1 || nn > kLuMaxNN) return pjg_internal_fail(PJG_ERR_UNSUPPORTED, "LU: nn must be in [1, 169]");
+    if (nn < 1 || nn > kBigMaxNN) return pjg_internal_fail(PJG_ERR_UNSUPPORTED, "LU: nn must be in [1, 4096]");
     if (n < 0) return pjg_internal_fail(PJG_ERR_ARG, "negative problem size");
     if (order != 'C' && order != 'F') return pjg_internal_fail(PJG_ERR_ARG, "order must be 'C' or 'F'");
     if (n == 0) return 0;
     if (!lu || !piv || !b) return pjg_internal_fail(PJG_ERR_ARG, "null array");
     const int grid = (int)((n + 127) / 128);
-    if (order == 'F')
+    if (nn > kSolveNMax) {
+        int rc;
+        if (nn <= 4 * kSolveThreads) rc = lu_solve_big_launch<4>(nn, n, order, lu, piv, b, st);
+        else if (nn <= 8 * kSolveThreads) rc = lu_solve_big_launch<8>(nn, n, order, lu, piv, b, st);
+        else if (nn <= 16 * kSolveThreads) rc = lu_solve_big_launch<16>(nn, n, order, lu, piv, b, st);
+        else rc = lu_solve_big_launch<32>(nn, n, order, lu, piv, b, st);
+        if (rc) return rc;
+    } else if (order == 'F')
         lu_solve_kernel<true><<<grid, 128, 0, st>>>(nn, n, lu, piv, b);
     else
         lu_solve_kernel<false><<<grid, 128, 0, st>>>(nn, n, lu, piv, b);

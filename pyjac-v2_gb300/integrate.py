@@ -8,7 +8,9 @@ pjg_lu_factor, pjg_lu_solve, pjg_lu_factor_sparse, pjg_lu_solve_sparse,
 pjg_ros2_step) on the current torch stream.
 
 Two factorisations: partial pivoting (LAPACK dgetf2's algorithm, any dense
-matrix up to 169 x 169), and the static-pivot sparse LU of implicit chemistry
+matrix up to 4096 x 4096: in shared memory up to 169, above that blocked in
+global memory with the same operations), and the static-pivot sparse LU of
+implicit chemistry
 solvers (KPP): rows and columns ordered once by the Markowitz rule on the
 mechanism's Jacobian pattern, no interchanges, only the filled pattern
 updated (GRI-Mech 3.0: 19,752 FMAs per state instead of 51,039).

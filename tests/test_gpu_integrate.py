@@ -122,9 +122,49 @@ def test_empty_and_unsupported_sizes(cuda_device):
     z = torch.zeros((0, 10, 10), dtype=torch.float64, device=cuda_device)
     lu, piv, info = integ.lu_factor(z, 1e-6)
     assert lu.numel() == 0 and piv.numel() == 0 and info.numel() == 0
-    big = torch.zeros((1, 170, 170), dtype=torch.float64, device=cuda_device)
+    big = torch.zeros((1, 4097, 4097), dtype=torch.float64, device=cuda_device)
     with pytest.raises(RuntimeError, match="nn must be in"):
         integ.lu_factor(big, 1e-6)
+
+
+@pytest.mark.parametrize("order", ["C", "F"])
+@pytest.mark.parametrize("nn", [170, 177, 257, 501])
+def test_lu_factor_global_memory_sizes_bitwise(cuda_device, order, nn):
+    """Matrices beyond shared memory (nn > 169): the blocked global-memory
+    factorisation performs the oracle's operations in the same order, so the
+    factors, pivots and solves are identical; 501 is the synthetic
+    500-species mechanism's size.  Also in place, with a zero column, and
+    with the vector solve beyond the local-array solve (nn > 176)."""
+    import torch
+    orc = oracle_mod()
+    integ = pkg("integrate")
+    rng = np.random.default_rng(nn)
+    n = 6
+    J = rng.standard_normal((n, nn, nn)) * 10.0 ** rng.uniform(-3, 3, (n, 1, nn))
+    h = 10.0 ** rng.uniform(-1, 0, n)
+    # state 1: an exactly zero column of M = I - h J (h = 1, J's column the
+    # unit vector), so info reports the first zero pivot
+    J[1, :, nn // 3] = 0.0
+    J[1, nn // 3, nn // 3] = 1.0
+    h[1] = 1.0
+    lu_ref, piv_ref, info_ref = orc.lu_factor(J, 1.0, h)
+    assert info_ref[1] != 0
+    t = _to_dev_mat(J, order, cuda_device)
+    hd = torch.from_numpy(h).to(cuda_device)
+    lu, piv, info = integ.lu_factor(t, hd, order=order)
+    assert np.array_equal(_from_dev_mat(lu, order), lu_ref)
+    assert np.array_equal(_from_dev_vec(piv, order), piv_ref)
+    assert np.array_equal(info.cpu().numpy(), info_ref)
+    lu2, _, _ = integ.lu_factor(t, hd, order=order, out=t)  # in place
+    assert lu2.data_ptr() == t.data_ptr()
+    assert np.array_equal(_from_dev_mat(lu2, order), lu_ref)
+    b = rng.standard_normal((n, nn))
+    keep = [0, 2, 3, 4, 5]  # solves with a nonsingular factor
+    x_ref = orc.lu_solve(lu_ref[keep], piv_ref[keep], b[keep])
+    x = integ.lu_solve(_to_dev_mat(lu_ref[keep], order, cuda_device),
+                       _to_dev_vec(piv_ref[keep], order, cuda_device),
+                       _to_dev_vec(b[keep], order, cuda_device), order=order)
+    assert np.array_equal(_from_dev_vec(x, order), x_ref)
 
 
 @pytest.mark.parametrize("order", ["C", "F"])
