@@ -407,6 +407,10 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
             a.s01 = t->s01;
             a.s10 = t->s10;
             a.s11 = t->s11;
+            if (jac_format != PJG_JAC_SPARSE) {
+                a.dense_rs = F ? 1 : NN;
+                a.dense_cs = F ? NN : 1;
+            }
         }
         int rc = 0;
         if (kind == PJG_JACOBIAN) {

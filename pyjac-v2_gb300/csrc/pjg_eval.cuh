@@ -57,6 +57,9 @@ struct EvalArgs {
     const int* sp_slots;      // 2 per species row: slot(k, T), slot(k, E)
     const int* cj_slots;      // 2 per species column: slot(T, j), slot(E, j)
     int s00, s01, s10, s11;
+    // dense output: slot of (row r, column c) = r * dense_rs + c * dense_cs
+    // (0, 0 for a sparse output, whose slots come from the tables)
+    int dense_rs, dense_cs;
     // vector-Jacobian product
     const double* v;          // v[s * phi_ss + j * phi_sj]
     double* vjp;              // same layout
