@@ -21,6 +21,7 @@
 #include "../../include/pyjac_gb300.h"
 #include "../../include/pyjac_gb300_internal.h"
 #include "pjg_eval.cuh"
+#include "pjg_rxn.cuh"
 #include "pjg_mlp.cuh"
 
 namespace {
@@ -85,6 +86,7 @@ extern "C" int pjg_internal_lu_solve_sparse(const void* p, int64_t n, char order
 struct pjg_mech {
     int ns = 0, nr = 0, nn = 0, need_logP = 0, nnz = 0, jac_approx = 0;
     int nr_e22 = 0;  // leading reactions of the class A + B <=> C + D
+    int ma_off[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // then the mass-action patterns (EvalArgs)
     int device = 0;
     PjgRxn* rxn = nullptr;
     double* sp = nullptr;
@@ -303,6 +305,7 @@ void fill_common(const pjg_mech* m, EvalArgs& a)
     a.ns = m->ns;
     a.nr = m->nr;
     a.nr_e22 = m->nr_e22;
+    for (int q = 0; q <= pjg::kMaPatterns; ++q) a.ma_off[q] = m->ma_off[q];
     a.need_logP = m->need_logP;
     a.jac_approx = m->jac_approx;
 }
@@ -442,6 +445,118 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
     }
     return 0;
 }
+
+// A reaction of the class A + B <=> C + D: four distinct species with unit
+// coefficients, reversible, an Arrhenius rate form, no third body, and
+// (P_atm / R)^nu_sum = 1 (nu_sum = 0).  241 of GRI-Mech 3.0's 325 reactions.
+bool is_e22(const PjgRxn& R)
+{
+    if (R.nspec != 4 || RX_FORM(R.flags) > FORM_ARR || !(R.flags & RX_REV) ||
+        RX_THD(R.flags) != THD_NONE || R.nu_sum != 0 || R.p[P_PSUM] != 1.0)
+        return false;
+    int nre = 0, npr = 0;
+    for (int e = 0; e < 4; ++e) {
+        const int f = ent_nuf(R.ent[e]), r = ent_nur(R.ent[e]);
+        if (f == 1 && r == 0) ++nre;
+        else if (f == 0 && r == 1) ++npr;
+        else return false;
+    }
+    return nre == 2 && npr == 2;
+}
+
+// The (coefficient pattern) of a reaction without third body, Arrhenius form:
+// its entries as (reactant, product) coefficients, reactants first by
+// coefficient, then products by coefficient.  Returns the index of the
+// matching MaPattern, or -1 (entries on both sides, coefficients above 2,
+// third bodies, fall-off, PLOG and Chebyshev keep the general code).
+template <class PT>
+bool ma_matches(const std::vector<std::pair<int, int>>& key, bool rev)
+{
+    if (PT::rev != rev || (int)key.size() != PT::n) return false;
+    for (int e = 0; e < PT::n; ++e)
+        if (key[e].first != PT::nuf(e) || key[e].second != PT::nur(e)) return false;
+    return true;
+}
+
+int ma_pattern_of(const PjgRxn& R)
+{
+    if (RX_FORM(R.flags) > FORM_ARR || RX_THD(R.flags) != THD_NONE || R.nspec < 3 || R.nspec > 5)
+        return -1;
+    std::vector<std::pair<int, int>> key;
+    for (int side = 0; side < 2; ++side)
+        for (int nu = 1; nu <= 2; ++nu)
+            for (int e = 0; e < R.nspec; ++e) {
+                const int f = ent_nuf(R.ent[e]), r = ent_nur(R.ent[e]);
+                if (side == 0 && f == nu && r == 0) key.push_back({f, 0});
+                if (side == 1 && r == nu && f == 0) key.push_back({0, r});
+            }
+    if ((int)key.size() != R.nspec) return -1;  // a species on both sides, or a coefficient > 2
+    const bool rev = R.flags & RX_REV;
+    if (ma_matches<pjg::MaP0>(key, rev)) return 0;
+    if (ma_matches<pjg::MaP1>(key, rev)) return 1;
+    if (ma_matches<pjg::MaP2>(key, rev)) return 2;
+    if (ma_matches<pjg::MaP3>(key, rev)) return 3;
+    if (ma_matches<pjg::MaP4>(key, rev)) return 4;
+    if (ma_matches<pjg::MaP5>(key, rev)) return 5;
+    if (ma_matches<pjg::MaP6>(key, rev)) return 6;
+    if (ma_matches<pjg::MaP7>(key, rev)) return 7;
+    return -1;
+}
+
+// Reactions of the class above go first, each with its entries reordered
+// reactants first (species order kept within each side), so that the kernels
+// evaluate them by straight-line code with coefficients known at compile
+// time; the others follow in mechanism order.  Nothing outside the kernels
+// depends on the reaction order: the species rates and the Jacobian are sums
+// over reactions, and the slot tables are built from these records.
+void order_reactions(pjg_mech* m)
+{
+    std::vector<PjgRxn> head, tail;
+    for (const PjgRxn& R : m->h_rxn) {
+        if (!is_e22(R)) {
+            tail.push_back(R);
+            continue;
+        }
+        PjgRxn c = R;
+        int q = 0;
+        for (int side = 0; side < 2; ++side)
+            for (int e = 0; e < 4; ++e)
+                if ((ent_nuf(R.ent[e]) == 1) == (side == 0)) c.ent[q++] = R.ent[e];
+        head.push_back(c);
+    }
+    m->nr_e22 = (int)head.size();
+    // then the mass-action patterns MaP0..MaP7 (pjg_rxn.cuh), entries in the
+    // pattern's order: reactants by coefficient, then products by
+    // coefficient (species order kept among equal coefficients)
+    std::vector<PjgRxn> rest;
+    std::vector<std::vector<PjgRxn>> byp(pjg::kMaPatterns);
+    for (const PjgRxn& R : tail) {
+        const int q = ma_pattern_of(R);
+        if (q < 0) {
+            rest.push_back(R);
+            continue;
+        }
+        PjgRxn c = R;
+        int k = 0;
+        for (int side = 0; side < 2; ++side)
+            for (int nu = 1; nu <= 2; ++nu)
+                for (int e = 0; e < R.nspec; ++e)
+                    if ((side == 0 ? ent_nuf(R.ent[e]) : ent_nur(R.ent[e])) == nu &&
+                        (side == 0 ? ent_nur(R.ent[e]) : ent_nuf(R.ent[e])) == 0)
+                        c.ent[k++] = R.ent[e];
+        byp[q].push_back(c);
+    }
+    int pos = m->nr_e22;
+    for (int q = 0; q < pjg::kMaPatterns; ++q) {
+        m->ma_off[q] = pos;
+        head.insert(head.end(), byp[q].begin(), byp[q].end());
+        pos += (int)byp[q].size();
+    }
+    m->ma_off[pjg::kMaPatterns] = pos;
+    head.insert(head.end(), rest.begin(), rest.end());
+    m->h_rxn.swap(head);
+}
+
 
 }  // namespace
 
@@ -639,53 +754,6 @@ int pjg_profile_end(int64_t* launches, double* total_ms)
     return rc;
 }
 
-namespace {
-
-// A reaction of the class A + B <=> C + D: four distinct species with unit
-// coefficients, reversible, an Arrhenius rate form, no third body, and
-// (P_atm / R)^nu_sum = 1 (nu_sum = 0).  241 of GRI-Mech 3.0's 325 reactions.
-bool is_e22(const PjgRxn& R)
-{
-    if (R.nspec != 4 || RX_FORM(R.flags) > FORM_ARR || !(R.flags & RX_REV) ||
-        RX_THD(R.flags) != THD_NONE || R.nu_sum != 0 || R.p[P_PSUM] != 1.0)
-        return false;
-    int nre = 0, npr = 0;
-    for (int e = 0; e < 4; ++e) {
-        const int f = ent_nuf(R.ent[e]), r = ent_nur(R.ent[e]);
-        if (f == 1 && r == 0) ++nre;
-        else if (f == 0 && r == 1) ++npr;
-        else return false;
-    }
-    return nre == 2 && npr == 2;
-}
-
-// Reactions of the class above go first, each with its entries reordered
-// reactants first (species order kept within each side), so that the kernels
-// evaluate them by straight-line code with coefficients known at compile
-// time; the others follow in mechanism order.  Nothing outside the kernels
-// depends on the reaction order: the species rates and the Jacobian are sums
-// over reactions, and the slot tables are built from these records.
-void order_reactions(pjg_mech* m)
-{
-    std::vector<PjgRxn> head, tail;
-    for (const PjgRxn& R : m->h_rxn) {
-        if (!is_e22(R)) {
-            tail.push_back(R);
-            continue;
-        }
-        PjgRxn c = R;
-        int q = 0;
-        for (int side = 0; side < 2; ++side)
-            for (int e = 0; e < 4; ++e)
-                if ((ent_nuf(R.ent[e]) == 1) == (side == 0)) c.ent[q++] = R.ent[e];
-        head.push_back(c);
-    }
-    m->nr_e22 = (int)head.size();
-    head.insert(head.end(), tail.begin(), tail.end());
-    m->h_rxn.swap(head);
-}
-
-}  // namespace
 
 int pjg_mech_create(const pjg_tables* tb, pjg_mech** out)
 {

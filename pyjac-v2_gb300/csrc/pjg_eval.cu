@@ -214,8 +214,66 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         }
     }
 
+    // ------------------------- other mass-action reactions in fixed patterns
+    auto ma_range = [&](auto tag, int i0, int i1) {
+        using PT = decltype(tag);
+        constexpr int N = PT::n;
+        for (int i = i0; i < i1; ++i) {
+            RxnHead h;
+            load_head(a.rxn + i, h);
+            MaTerms o;
+            ma_terms<PT, DER>(h, last, sv, conc, bk, db, o);
+            int sp[N];
+#pragma unroll
+            for (int e = 0; e < N; ++e) {
+                sp[e] = ent_spec(h.ent[e]);
+                accum(wdot, sp[e], nux(PT::nur(e) - PT::nuf(e), o.net));
+            }
+            if (!DER) continue;
+            const bool hasns = (h.flags & RX_HASNS) && !a.jac_approx;
+            if (VJP) {
+                double w = 0.0;
+#pragma unroll
+                for (int ka = 0; ka < N; ++ka)
+                    if (sp[ka] != last) w = addnu(w, PT::nur(ka) - PT::nuf(ka), hw[sp[ka]]);
+                if (w != 0.0) {
+#pragma unroll
+                    for (int jb = 0; jb < N; ++jb)
+                        if (sp[jb] != last) accum(nsrow, sp[jb], w * o.g[jb]);
+                    if (hasns) vNS = fma(w, o.gns, vNS);
+                    vout0 = fma(w, o.d0, vout0);
+                    vout1 = fma(w, o.d1, vout1);
+                }
+                continue;
+            }
+            const int* slots = a.rxn_slots + __ldg(a.rxn_slot_off + i);
+            double* accs = a.acc + s;
+#pragma unroll
+            for (int ka = 0; ka < N; ++ka) {
+                const int nuk = PT::nur(ka) - PT::nuf(ka);
+                if (sp[ka] == last) continue;
+#pragma unroll
+                for (int jb = 0; jb < N + 2; ++jb) {
+                    const int sl = jb < N ? __ldg(slots + ka * N + jb)
+                                          : __ldg(slots + N * N + 2 * ka + (jb - N));
+                    const double v = jb < N ? o.g[jb] : (jb == N ? o.d0 : o.d1);
+                    if (sl >= 0) atomicAdd(accs + (int64_t)sl * a.acc_ld, nux(nuk, v));
+                }
+                if (hasns) accum(nsrow, sp[ka], nux(nuk, o.gns));
+            }
+        }
+    };
+    ma_range(MaP0{}, a.ma_off[0], a.ma_off[1]);
+    ma_range(MaP1{}, a.ma_off[1], a.ma_off[2]);
+    ma_range(MaP2{}, a.ma_off[2], a.ma_off[3]);
+    ma_range(MaP3{}, a.ma_off[3], a.ma_off[4]);
+    ma_range(MaP4{}, a.ma_off[4], a.ma_off[5]);
+    ma_range(MaP5{}, a.ma_off[5], a.ma_off[6]);
+    ma_range(MaP6{}, a.ma_off[6], a.ma_off[7]);
+    ma_range(MaP7{}, a.ma_off[7], a.ma_off[8]);
+
     // ------------------------------------------------------- other reactions
-    for (int i = a.nr_e22; i < a.nr; ++i) {
+    for (int i = a.ma_off[kMaPatterns]; i < a.nr; ++i) {
         RxnHead h;
         load_head(a.rxn + i, h);
         RxnTerms o;

@@ -30,6 +30,8 @@ struct EvalArgs {
     const double* aux;
     int ns, nr;
     int nr_e22;      // reactions [0, nr_e22) are of the class A + B <=> C + D (see pjg_rxn.cuh)
+    int ma_off[9];   // then [ma_off[q], ma_off[q + 1]) of mass-action pattern q (MaP0..MaP7),
+                     // ma_off[0] = nr_e22; the others from ma_off[8]
     int need_logP;
     int jac_approx;  // 'approximate' Jacobian type: no bath-gas terms in the species columns
     // states

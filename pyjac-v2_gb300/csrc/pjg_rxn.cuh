@@ -426,4 +426,137 @@ __device__ __forceinline__ void e22_terms(const E22Head& h, int last, const Stat
     o.d1 = d1;
 }
 
+// ------------------------------------------------------------------------
+// Other mass-action reactions without a third body, in a few fixed
+// stoichiometric patterns (MaPattern below; pjg_capi.cu order_reactions packs
+// each pattern's reactions together, entries in the pattern's order:
+// reactants by coefficient, then products by coefficient).  The arithmetic
+// of rxn_terms() for such a reaction with every coefficient known at compile
+// time.  Up to five entries.
+template <bool REV, int F0, int R0, int F1, int R1, int F2, int R2, int F3 = 0, int R3 = 0,
+          int F4 = 0, int R4 = 0>
+struct MaPattern {
+    static constexpr bool rev = REV;
+    static constexpr int n = (F4 || R4) ? 5 : (F3 || R3) ? 4 : 3;
+    __host__ __device__ static constexpr int nuf(int e)
+    {
+        return e == 0 ? F0 : e == 1 ? F1 : e == 2 ? F2 : e == 3 ? F3 : F4;
+    }
+    __host__ __device__ static constexpr int nur(int e)
+    {
+        return e == 0 ? R0 : e == 1 ? R1 : e == 2 ? R2 : e == 3 ? R3 : R4;
+    }
+    __host__ __device__ static constexpr int sumf() { return F0 + F1 + F2 + F3 + F4; }
+    __host__ __device__ static constexpr int sumr() { return R0 + R1 + R2 + R3 + R4; }
+};
+
+// the patterns, in the order their reactions are packed (kMaPatterns of them)
+using MaP0 = MaPattern<false, 1, 0, 1, 0, 0, 1, 0, 1, 0, 1>;  // A + B => C + D + E
+using MaP1 = MaPattern<true, 1, 0, 1, 0, 0, 1, 0, 1, 0, 1>;   // A + B <=> C + D + E
+using MaP2 = MaPattern<true, 1, 0, 1, 0, 0, 2>;               // A + B <=> 2 C
+using MaP3 = MaPattern<true, 2, 0, 0, 1, 0, 1>;               // 2 A <=> B + C
+using MaP4 = MaPattern<true, 1, 0, 1, 0, 1, 0, 0, 1, 0, 1>;   // A + B + C <=> D + E
+using MaP5 = MaPattern<true, 1, 0, 1, 0, 0, 1, 0, 2>;         // A + B <=> C + 2 D
+using MaP6 = MaPattern<true, 1, 0, 2, 0, 0, 1, 0, 1>;         // A + 2 B <=> C + D
+using MaP7 = MaPattern<false, 1, 0, 1, 0, 0, 1, 0, 1>;        // A + B => C + D
+constexpr int kMaPatterns = 8;
+
+// acc * v^p for a compile-time p (0, 1 or 2), rounded products
+template <int P>
+__device__ __forceinline__ double mulpow_rn(double acc, double v)
+{
+    if (P == 0) return acc;
+    if (P == 1) return __dmul_rn(acc, v);
+    return __dmul_rn(acc, __dmul_rn(v, v));
+}
+
+struct MaTerms {
+    double net;
+    double g[5];
+    double gns;
+    double d0, d1;
+};
+
+template <class PT, bool DER, class ARR>
+__device__ __forceinline__ void ma_terms(const RxnHead& h, int last, const StateVars& sv,
+                                         const ARR& conc, const ARR& bk, const ARR& db, MaTerms& o)
+{
+    constexpr int N = PT::n;
+    const double* p = h.p;
+    const double b = ldg(p + P_B), Ta = ldg(p + P_TA);
+    const double kf = arrhenius(RX_FORM(h.flags), ldg(p + P_A), b, Ta, h.bint, sv.Tc, sv.logT,
+                                sv.Tinv, sv.etab);
+    int sp[N];
+    double c[N];
+#pragma unroll
+    for (int e = 0; e < N; ++e) {
+        sp[e] = ent_spec(h.ent[e]);
+        c[e] = conc[sp[e]];
+    }
+    double kr = 0.0, dB = 0.0;
+    if (PT::rev) {
+        double Bsum = 0.0;
+#pragma unroll
+        for (int e = 0; e < N; ++e) {
+            Bsum = addnu(Bsum, PT::nur(e) - PT::nuf(e), bk[sp[e]]);
+            if (DER) dB = addnu(dB, PT::nur(e) - PT::nuf(e), db[sp[e]]);
+        }
+        kr = kf * ldg(p + P_PSUM) * fexp(-fmin(EXP_MAX, Bsum), sv.etab);
+    }
+    // rounded products and difference: the rate of progress is the same in
+    // every kernel kind (see e22_terms)
+    double rf = kf, rr = kr;
+#pragma unroll
+    for (int e = 0; e < N; ++e) {
+        if (PT::nuf(e) == 1) rf = mulpow_rn<1>(rf, c[e]);
+        if (PT::nuf(e) == 2) rf = mulpow_rn<2>(rf, c[e]);
+        if (PT::rev && PT::nur(e) == 1) rr = mulpow_rn<1>(rr, c[e]);
+        if (PT::rev && PT::nur(e) == 2) rr = mulpow_rn<2>(rr, c[e]);
+    }
+    o.net = PT::rev ? __dsub_rn(rf, rr) : rf;
+    if (!DER) return;
+    const double dlnkf_dT = (b + Ta * sv.Tjinv) * sv.Tjinv;
+    double cg[N];
+#pragma unroll
+    for (int e = 0; e < N; ++e) cg[e] = gsmall(c[e]);
+    double gns = 0.0;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        double gf = 0.0, gr = 0.0;
+        if (PT::nuf(j)) {
+            double S = PT::nuf(j) == 2 ? kf + kf : kf;
+#pragma unroll
+            for (int e = 0; e < N; ++e) {
+                const int q = PT::nuf(e) - (e == j);
+                if (q == 1) S = S * cg[e];
+                if (q == 2) S = S * (cg[e] * cg[e]);
+            }
+            gf = S;
+        }
+        if (PT::rev && PT::nur(j)) {
+            double S = PT::nur(j) == 2 ? kr + kr : kr;
+#pragma unroll
+            for (int e = 0; e < N; ++e) {
+                const int q = PT::nur(e) - (e == j);
+                if (q == 1) S = S * cg[e];
+                if (q == 2) S = S * (cg[e] * cg[e]);
+            }
+            gr = S;
+        }
+        o.g[j] = gf - gr;
+        if (sp[j] == last) gns = o.g[j];
+    }
+    o.gns = gns;
+    const bool hasns = h.flags & RX_HASNS;
+    double d0 = rf * dlnkf_dT;
+    if (PT::rev) d0 = d0 + -1.0 * rr * (dlnkf_dT + -1.0 * dB);
+    d0 = d0 * sv.V;
+    if (hasns) d0 += -gns * sv.V * sv.PoRT * sv.Tjinv;
+    double d1 = 0.0;
+    if (sv.conp) d1 = -nux(PT::sumf() - 1, rf) + (PT::rev ? nux(PT::sumr() - 1, rr) : 0.0);
+    if (hasns) d1 += gns * (sv.conp ? sv.PoRT : sv.V * sv.rt_inv);
+    o.d0 = d0;
+    o.d1 = d1;
+}
+
 }  // namespace pjg
