@@ -87,6 +87,7 @@ struct pjg_mech {
     int ns = 0, nr = 0, nn = 0, need_logP = 0, nnz = 0, jac_approx = 0;
     int nr_e22 = 0;  // leading reactions of the class A + B <=> C + D
     int ma_off[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // then the mass-action patterns (EvalArgs)
+    int tp_off[4] = {0, 0, 0, 0};                 // then the third-body patterns (EvalArgs)
     int device = 0;
     PjgRxn* rxn = nullptr;
     double* sp = nullptr;
@@ -306,6 +307,7 @@ void fill_common(const pjg_mech* m, EvalArgs& a)
     a.nr = m->nr;
     a.nr_e22 = m->nr_e22;
     for (int q = 0; q <= pjg::kMaPatterns; ++q) a.ma_off[q] = m->ma_off[q];
+    for (int q = 0; q <= pjg::kTpPatterns; ++q) a.tp_off[q] = m->tp_off[q];
     a.need_logP = m->need_logP;
     a.jac_approx = m->jac_approx;
 }
@@ -464,11 +466,8 @@ bool is_e22(const PjgRxn& R)
     return nre == 2 && npr == 2;
 }
 
-// The (coefficient pattern) of a reaction without third body, Arrhenius form:
-// its entries as (reactant, product) coefficients, reactants first by
-// coefficient, then products by coefficient.  Returns the index of the
-// matching MaPattern, or -1 (entries on both sides, coefficients above 2,
-// third bodies, fall-off, PLOG and Chebyshev keep the general code).
+// whether a canonical coefficient list (pattern_key) and reversibility are
+// those of the pattern PT (pjg_rxn.cuh)
 template <class PT>
 bool ma_matches(const std::vector<std::pair<int, int>>& key, bool rev)
 {
@@ -478,10 +477,11 @@ bool ma_matches(const std::vector<std::pair<int, int>>& key, bool rev)
     return true;
 }
 
-int ma_pattern_of(const PjgRxn& R)
+// the canonical (reactant, product) coefficient list of a record: reactant
+// entries by coefficient, then product entries by coefficient; empty if a
+// species is on both sides or a coefficient is above 2
+std::vector<std::pair<int, int>> pattern_key(const PjgRxn& R)
 {
-    if (RX_FORM(R.flags) > FORM_ARR || RX_THD(R.flags) != THD_NONE || R.nspec < 3 || R.nspec > 5)
-        return -1;
     std::vector<std::pair<int, int>> key;
     for (int side = 0; side < 2; ++side)
         for (int nu = 1; nu <= 2; ++nu)
@@ -490,7 +490,47 @@ int ma_pattern_of(const PjgRxn& R)
                 if (side == 0 && f == nu && r == 0) key.push_back({f, 0});
                 if (side == 1 && r == nu && f == 0) key.push_back({0, r});
             }
-    if ((int)key.size() != R.nspec) return -1;  // a species on both sides, or a coefficient > 2
+    if ((int)key.size() != R.nspec) key.clear();
+    return key;
+}
+
+// TpP0..TpP2: third-body or fall-off reactions of an Arrhenius form
+int tp_pattern_of(const PjgRxn& R)
+{
+    if (RX_FORM(R.flags) > FORM_ARR || RX_THD(R.flags) == THD_NONE) return -1;
+    const auto key = pattern_key(R);
+    const bool rev = R.flags & RX_REV;
+    if (key.empty()) return -1;
+    if (ma_matches<pjg::TpP0>(key, rev)) return 0;
+    if (ma_matches<pjg::TpP1>(key, rev)) return 1;
+    if (ma_matches<pjg::TpP2>(key, rev)) return 2;
+    return -1;
+}
+
+// the record with its entries in the canonical order of pattern_key
+PjgRxn canonical_entries(const PjgRxn& R)
+{
+    PjgRxn c = R;
+    int k = 0;
+    for (int side = 0; side < 2; ++side)
+        for (int nu = 1; nu <= 2; ++nu)
+            for (int e = 0; e < R.nspec; ++e)
+                if ((side == 0 ? ent_nuf(R.ent[e]) : ent_nur(R.ent[e])) == nu &&
+                    (side == 0 ? ent_nur(R.ent[e]) : ent_nuf(R.ent[e])) == 0)
+                    c.ent[k++] = R.ent[e];
+    return c;
+}
+
+// MaP0..MaP7: reactions without third body, of an Arrhenius form, whose
+// canonical coefficient list matches a pattern; -1 otherwise (entries on both
+// sides, coefficients above 2, third bodies, fall-off, PLOG and Chebyshev
+// keep the general code)
+int ma_pattern_of(const PjgRxn& R)
+{
+    if (RX_FORM(R.flags) > FORM_ARR || RX_THD(R.flags) != THD_NONE || R.nspec < 3 || R.nspec > 5)
+        return -1;
+    const auto key = pattern_key(R);
+    if (key.empty()) return -1;  // a species on both sides, or a coefficient > 2
     const bool rev = R.flags & RX_REV;
     if (ma_matches<pjg::MaP0>(key, rev)) return 0;
     if (ma_matches<pjg::MaP1>(key, rev)) return 1;
@@ -528,23 +568,14 @@ void order_reactions(pjg_mech* m)
     // then the mass-action patterns MaP0..MaP7 (pjg_rxn.cuh), entries in the
     // pattern's order: reactants by coefficient, then products by
     // coefficient (species order kept among equal coefficients)
+    // then the third-body patterns TpP0..TpP2, the same entry order
     std::vector<PjgRxn> rest;
-    std::vector<std::vector<PjgRxn>> byp(pjg::kMaPatterns);
+    std::vector<std::vector<PjgRxn>> byp(pjg::kMaPatterns), byt(pjg::kTpPatterns);
     for (const PjgRxn& R : tail) {
-        const int q = ma_pattern_of(R);
-        if (q < 0) {
-            rest.push_back(R);
-            continue;
-        }
-        PjgRxn c = R;
-        int k = 0;
-        for (int side = 0; side < 2; ++side)
-            for (int nu = 1; nu <= 2; ++nu)
-                for (int e = 0; e < R.nspec; ++e)
-                    if ((side == 0 ? ent_nuf(R.ent[e]) : ent_nur(R.ent[e])) == nu &&
-                        (side == 0 ? ent_nur(R.ent[e]) : ent_nuf(R.ent[e])) == 0)
-                        c.ent[k++] = R.ent[e];
-        byp[q].push_back(c);
+        const int q = ma_pattern_of(R), t = q < 0 ? tp_pattern_of(R) : -1;
+        if (q >= 0) byp[q].push_back(canonical_entries(R));
+        else if (t >= 0) byt[t].push_back(canonical_entries(R));
+        else rest.push_back(R);
     }
     int pos = m->nr_e22;
     for (int q = 0; q < pjg::kMaPatterns; ++q) {
@@ -553,6 +584,12 @@ void order_reactions(pjg_mech* m)
         pos += (int)byp[q].size();
     }
     m->ma_off[pjg::kMaPatterns] = pos;
+    for (int q = 0; q < pjg::kTpPatterns; ++q) {
+        m->tp_off[q] = pos;
+        head.insert(head.end(), byt[q].begin(), byt[q].end());
+        pos += (int)byt[q].size();
+    }
+    m->tp_off[pjg::kTpPatterns] = pos;
     head.insert(head.end(), rest.begin(), rest.end());
     m->h_rxn.swap(head);
 }

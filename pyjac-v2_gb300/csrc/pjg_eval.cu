@@ -273,101 +273,110 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     ma_range(MaP7{}, a.ma_off[7], a.ma_off[8]);
 
     // ------------------------------------------------------- other reactions
-    for (int i = a.ma_off[kMaPatterns]; i < a.nr; ++i) {
-        RxnHead h;
-        load_head(a.rxn + i, h);
-        RxnTerms o;
-        rxn_terms<DER>(h, a.aux, a.thd_spec, a.thd_coef, last, sv, conc, bk, db, o);
-        const int flags = h.flags, nsp = h.nsp, thd_off = h.thd_off, thd_cnt = h.thd_cnt;
-        const unsigned* ent = h.ent;
-        const double* p = h.p;
+    // (the general code; third-body and fall-off reactions of the patterns
+    // TpP0..TpP2 compiled per pattern, the rest reading their coefficients)
+    auto general = [&](auto st_tag, int i0, int i1) {
+        using ST = decltype(st_tag);
+        for (int i = i0; i < i1; ++i) {
+            RxnHead h;
+            load_head(a.rxn + i, h);
+            RxnTerms o;
+            rxn_terms<DER, ST>(h, a.aux, a.thd_spec, a.thd_coef, last, sv, conc, bk, db, o);
+            const int flags = h.flags, nsp = ST::nsp(h), thd_off = h.thd_off, thd_cnt = h.thd_cnt;
+            const unsigned* ent = h.ent;
+            const double* p = h.p;
 #pragma unroll
-        for (int e = 0; e < PJG_MAXSP; ++e) {
-            if (e >= nsp) break;
-            const int nu = ent_nur(ent[e]) - ent_nuf(ent[e]);
-            if (nu != 0) accum(wdot, ent_spec(ent[e]), nux(nu, o.net));
-        }
-        if (!DER) continue;
+            for (int e = 0; e < PJG_MAXSP; ++e) {
+                if (e >= nsp) break;
+                const int nu = ST::nur(h, e) - ST::nuf(h, e);
+                if (nu != 0) accum(wdot, ent_spec(ent[e]), nux(nu, o.net));
+            }
+            if (!DER) continue;
 
-        // ------------------------------------------------- Jacobian terms
-        const int* slots = JAC ? a.rxn_slots + __ldg(a.rxn_slot_off + i) : nullptr;
-        const int thd = RX_THD(flags);
-        const bool hasns = flags & RX_HASNS;
-        const double ci_ = o.ci_, X = o.X, d0 = o.d0, d1 = o.d1, gns = o.gns;
-        const double* g = o.g;
-        const double cns = ldg(p + P_CNS);
-        const bool nslist = flags & RX_NSLIST;
-        if (VJP) {
-            // w = sum_k nu_k vt_k over the species rows of this reaction
-            double w = 0.0;
+            // ------------------------------------------------- Jacobian terms
+            const int* slots = JAC ? a.rxn_slots + __ldg(a.rxn_slot_off + i) : nullptr;
+            const int thd = RX_THD(flags);
+            const bool hasns = flags & RX_HASNS;
+            const double ci_ = o.ci_, X = o.X, d0 = o.d0, d1 = o.d1, gns = o.gns;
+            const double* g = o.g;
+            const double cns = ldg(p + P_CNS);
+            const bool nslist = flags & RX_NSLIST;
+            if (VJP) {
+                // w = sum_k nu_k vt_k over the species rows of this reaction
+                double w = 0.0;
+#pragma unroll
+                for (int ka = 0; ka < PJG_MAXSP; ++ka) {
+                    if (ka >= nsp) break;
+                    const int k = ent_spec(ent[ka]);
+                    if (k == last) continue;
+                    w = addnu(w, ST::nur(h, ka) - ST::nuf(h, ka), hw[k]);
+                }
+                if (w != 0.0) {
+                    const double wc = w * ci_;
+#pragma unroll
+                    for (int jb = 0; jb < PJG_MAXSP; ++jb) {
+                        if (jb >= nsp) break;
+                        if (ent_spec(ent[jb]) != last) accum(nsrow, ent_spec(ent[jb]), wc * g[jb]);
+                    }
+                    if (hasns && !a.jac_approx) vNS = fma(wc, gns, vNS);
+                    if (thd) {
+                        const double wx = w * X;
+                        for (int l = 0; l < thd_cnt; ++l) {
+                            const int j = __ldg(a.thd_spec + thd_off + l);
+                            if (j != last) accum(nsrow, j, __ldg(a.thd_coef + thd_off + l) * wx);
+                        }
+                        if (nslist && !a.jac_approx) vNS = fma(cns, wx, vNS);
+                    }
+                    vout0 = fma(w, d0, vout0);
+                    vout1 = fma(w, d1, vout1);
+                }
+                continue;
+            }
+            // d R / d c_j times the pressure modification, once per reaction (ci is
+            // exactly 1 without a third body)
+            double gci[PJG_MAXSP];
+#pragma unroll
+            for (int e = 0; e < PJG_MAXSP; ++e) gci[e] = e < nsp ? (thd ? g[e] * ci_ : g[e]) : 0.0;
+            // scatter into the species rows of this reaction
 #pragma unroll
             for (int ka = 0; ka < PJG_MAXSP; ++ka) {
                 if (ka >= nsp) break;
                 const int k = ent_spec(ent[ka]);
                 if (k == last) continue;
-                w = addnu(w, ent_nur(ent[ka]) - ent_nuf(ent[ka]), hw[k]);
-            }
-            if (w != 0.0) {
-                const double wc = w * ci_;
+                const int nuk = ST::nur(h, ka) - ST::nuf(h, ka);
+                if (nuk == 0) continue;
+                // Fire-and-forget reductions (red.global.add.f64): the thread does not
+                // wait for the accumulator's old value.  Only this thread updates its
+                // state's entries, and one thread's operations on one address apply
+                // in program order, so every entry sums its reactions in a fixed order.
+                double* accs = a.acc + s;
 #pragma unroll
-                for (int jb = 0; jb < PJG_MAXSP; ++jb) {
-                    if (jb >= nsp) break;
-                    if (ent_spec(ent[jb]) != last) accum(nsrow, ent_spec(ent[jb]), wc * g[jb]);
+                for (int jb = 0; jb < PJG_MAXSP + 2; ++jb) {
+                    if (jb >= nsp + 2) break;
+                    const int sl = jb < nsp ? __ldg(slots + ka * nsp + jb)
+                                            : __ldg(slots + nsp * nsp + 2 * ka + (jb - nsp));
+                    const double v = jb < nsp ? gci[jb] : (jb == nsp ? d0 : d1);
+                    if (sl >= 0) atomicAdd(accs + (int64_t)sl * a.acc_ld, nux(nuk, v));
                 }
-                if (hasns && !a.jac_approx) vNS = fma(wc, gns, vNS);
+                double nsacc = 0.0;
+                if (hasns) nsacc = gns * ci_;
                 if (thd) {
-                    const double wx = w * X;
+                    const double wx = nux(nuk, X);
                     for (int l = 0; l < thd_cnt; ++l) {
-                        const int j = __ldg(a.thd_spec + thd_off + l);
-                        if (j != last) accum(nsrow, j, __ldg(a.thd_coef + thd_off + l) * wx);
+                        const int sl = __ldg(slots + nsp * nsp + 2 * nsp + l * nsp + ka);
+                        if (sl >= 0)
+                            atomicAdd(accs + (int64_t)sl * a.acc_ld, __ldg(a.thd_coef + thd_off + l) * wx);
                     }
-                    if (nslist && !a.jac_approx) vNS = fma(cns, wx, vNS);
+                    if (nslist) nsacc = fma(cns, X, nsacc);
                 }
-                vout0 = fma(w, d0, vout0);
-                vout1 = fma(w, d1, vout1);
+                if ((hasns || (thd && nslist)) && !a.jac_approx) accum(nsrow, k, nux(nuk, nsacc));
             }
-            continue;
         }
-        // d R / d c_j times the pressure modification, once per reaction (ci is
-        // exactly 1 without a third body)
-        double gci[PJG_MAXSP];
-#pragma unroll
-        for (int e = 0; e < PJG_MAXSP; ++e) gci[e] = e < nsp ? (thd ? g[e] * ci_ : g[e]) : 0.0;
-        // scatter into the species rows of this reaction
-#pragma unroll
-        for (int ka = 0; ka < PJG_MAXSP; ++ka) {
-            if (ka >= nsp) break;
-            const int k = ent_spec(ent[ka]);
-            if (k == last) continue;
-            const int nuk = ent_nur(ent[ka]) - ent_nuf(ent[ka]);
-            if (nuk == 0) continue;
-            // Fire-and-forget reductions (red.global.add.f64): the thread does not
-            // wait for the accumulator's old value.  Only this thread updates its
-            // state's entries, and one thread's operations on one address apply
-            // in program order, so every entry sums its reactions in a fixed order.
-            double* accs = a.acc + s;
-#pragma unroll
-            for (int jb = 0; jb < PJG_MAXSP + 2; ++jb) {
-                if (jb >= nsp + 2) break;
-                const int sl = jb < nsp ? __ldg(slots + ka * nsp + jb)
-                                        : __ldg(slots + nsp * nsp + 2 * ka + (jb - nsp));
-                const double v = jb < nsp ? gci[jb] : (jb == nsp ? d0 : d1);
-                if (sl >= 0) atomicAdd(accs + (int64_t)sl * a.acc_ld, nux(nuk, v));
-            }
-            double nsacc = 0.0;
-            if (hasns) nsacc = gns * ci_;
-            if (thd) {
-                const double wx = nux(nuk, X);
-                for (int l = 0; l < thd_cnt; ++l) {
-                    const int sl = __ldg(slots + nsp * nsp + 2 * nsp + l * nsp + ka);
-                    if (sl >= 0)
-                        atomicAdd(accs + (int64_t)sl * a.acc_ld, __ldg(a.thd_coef + thd_off + l) * wx);
-                }
-                if (nslist) nsacc = fma(cns, X, nsacc);
-            }
-            if ((hasns || (thd && nslist)) && !a.jac_approx) accum(nsrow, k, nux(nuk, nsacc));
-        }
-    }
+    };
+    general(PatStoich<TpP0>{}, a.tp_off[0], a.tp_off[1]);
+    general(PatStoich<TpP1>{}, a.tp_off[1], a.tp_off[2]);
+    general(PatStoich<TpP2>{}, a.tp_off[2], a.tp_off[3]);
+    general(RunStoich{}, a.tp_off[kTpPatterns], a.nr);
 
     __threadfence();
 

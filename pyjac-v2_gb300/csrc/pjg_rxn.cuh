@@ -97,18 +97,46 @@ struct RxnTerms {
     double X;                // third-body column factor, Rnet d ci / d [M]
 };
 
+// mulpow with rounded products: the rates of progress must not depend on
+// how the compiler contracts them into later FMAs, which differs between the
+// kernel kinds (the Jacobian kernel's rates equal the rates kernel's bit for
+// bit)
+__device__ __forceinline__ double mulpow_rn(double acc, double v, int p)
+{
+    if (p == 0) return acc;
+    if (p == 1) return __dmul_rn(acc, v);
+    if (p == 2) return __dmul_rn(acc, __dmul_rn(v, v));
+    return __dmul_rn(acc, powi(v, p));
+}
+
+// Stoichiometry of a reaction as rxn_terms() reads it: from the record
+// (RunStoich) or fixed at compile time by a coefficient pattern
+// (PatStoich<MaPattern<...>>, the record's entries stored in the pattern's
+// order).
+struct RunStoich {
+    __device__ static int nsp(const RxnHead& h) { return h.nsp; }
+    __device__ static int nuf(const RxnHead& h, int e) { return ent_nuf(h.ent[e]); }
+    __device__ static int nur(const RxnHead& h, int e) { return ent_nur(h.ent[e]); }
+};
+template <class PT>
+struct PatStoich {
+    __device__ static constexpr int nsp(const RxnHead&) { return PT::n; }
+    __device__ static constexpr int nuf(const RxnHead&, int e) { return PT::nuf(e); }
+    __device__ static constexpr int nur(const RxnHead&, int e) { return PT::nur(e); }
+};
+
 struct FallState {
     double Pr, Fi, A, B, Fc, lnFc, X, lnQ, kratio;
     double e1, e2, e3;  // Troe exponentials at the clamped temperature
 };
 
-template <bool DER, class ARR>
+template <bool DER, class ST = RunStoich, class ARR>
 __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                                           const int* thd_spec, const double* thd_coef, int last,
                                           const StateVars& sv, const ARR& conc, const ARR& bk,
                                           const ARR& db, RxnTerms& o)
 {
-    const int flags = h.flags, nsp = h.nsp;
+    const int flags = h.flags, nsp = ST::nsp(h);
     const double* p = h.p;
     const int form = RX_FORM(flags);
     const bool rev = flags & RX_REV;
@@ -135,7 +163,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
 #pragma unroll
         for (int e = 0; e < PJG_MAXSP; ++e) {
             if (e >= nsp) break;
-            const int nu = ent_nur(h.ent[e]) - ent_nuf(h.ent[e]);
+            const int nu = ST::nur(h, e) - ST::nuf(h, e);
             if (nu != 0) {
                 Bsum = addnu(Bsum, nu, bk[ent_spec(h.ent[e])]);
                 if (DER) dB = addnu(dB, nu, db[ent_spec(h.ent[e])]);
@@ -149,8 +177,8 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
     for (int e = 0; e < PJG_MAXSP; ++e) {
         if (e >= nsp) break;
         const double c = conc[ent_spec(h.ent[e])];
-        rf = mulpow(rf, c, ent_nuf(h.ent[e]));
-        if (rev) rr = mulpow(rr, c, ent_nur(h.ent[e]));
+        rf = mulpow_rn(rf, c, ST::nuf(h, e));
+        if (rev) rr = mulpow_rn(rr, c, ST::nur(h, e));
     }
     // third-body / fall-off pressure modification
     const int thd = RX_THD(flags);
@@ -210,7 +238,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
         }
     }
     double Rnet = rf;
-    if (rev) Rnet = Rnet + -1.0 * rr;
+    if (rev) Rnet = __dsub_rn(Rnet, rr);
     o.net = thd ? Rnet * ci : Rnet;
     if (!DER) return;
 
@@ -225,14 +253,14 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
 #pragma unroll
     for (int j = 0; j < PJG_MAXSP; ++j) {
         if (j >= nsp) break;
-        const int nfj = ent_nuf(h.ent[j]), nrj = ent_nur(h.ent[j]);
+        const int nfj = ST::nuf(h, j), nrj = ST::nur(h, j);
         double gf = 0.0, gr = 0.0;
         if (nfj) {
             double S = nux(nfj, kf);
 #pragma unroll
             for (int e = 0; e < PJG_MAXSP; ++e) {
                 if (e >= nsp) break;
-                S = mulpow(S, cg[e], ent_nuf(h.ent[e]) - (e == j));
+                S = mulpow(S, cg[e], ST::nuf(h, e) - (e == j));
             }
             gf = S;
         }
@@ -241,7 +269,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
 #pragma unroll
             for (int e = 0; e < PJG_MAXSP; ++e) {
                 if (e >= nsp) break;
-                S = mulpow(S, cg[e], ent_nur(h.ent[e]) - (e == j));
+                S = mulpow(S, cg[e], ST::nur(h, e) - (e == j));
             }
             gr = S;
         }
@@ -287,8 +315,8 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
 #pragma unroll
         for (int e = 0; e < PJG_MAXSP; ++e) {
             if (e >= nsp) break;
-            nuf += ent_nuf(h.ent[e]);
-            nur += ent_nur(h.ent[e]);
+            nuf += ST::nuf(h, e);
+            nur += ST::nur(h, e);
         }
         d1 = (-nux(nuf, rf) + (rev ? nux(nur, rr) : 0.0)) * ci_;
     } else if (form >= FORM_PLOG) {
@@ -433,11 +461,11 @@ __device__ __forceinline__ void e22_terms(const E22Head& h, int last, const Stat
 // reactants by coefficient, then products by coefficient).  The arithmetic
 // of rxn_terms() for such a reaction with every coefficient known at compile
 // time.  Up to five entries.
-template <bool REV, int F0, int R0, int F1, int R1, int F2, int R2, int F3 = 0, int R3 = 0,
+template <bool REV, int F0, int R0, int F1, int R1, int F2 = 0, int R2 = 0, int F3 = 0, int R3 = 0,
           int F4 = 0, int R4 = 0>
 struct MaPattern {
     static constexpr bool rev = REV;
-    static constexpr int n = (F4 || R4) ? 5 : (F3 || R3) ? 4 : 3;
+    static constexpr int n = 2 + (F2 || R2) + (F3 || R3) + (F4 || R4);
     __host__ __device__ static constexpr int nuf(int e)
     {
         return e == 0 ? F0 : e == 1 ? F1 : e == 2 ? F2 : e == 3 ? F3 : F4;
@@ -460,6 +488,13 @@ using MaP5 = MaPattern<true, 1, 0, 1, 0, 0, 1, 0, 2>;         // A + B <=> C + 2
 using MaP6 = MaPattern<true, 1, 0, 2, 0, 0, 1, 0, 1>;         // A + 2 B <=> C + D
 using MaP7 = MaPattern<false, 1, 0, 1, 0, 0, 1, 0, 1>;        // A + B => C + D
 constexpr int kMaPatterns = 8;
+
+// coefficient patterns of reactions with a third body or fall-off, evaluated
+// by the general code (rxn_terms) compiled per pattern (PatStoich)
+using TpP0 = MaPattern<true, 1, 0, 1, 0, 0, 1>;  // A + B (+M) <=> C
+using TpP1 = MaPattern<true, 1, 0, 0, 1, 0, 1>;  // A (+M) <=> B + C
+using TpP2 = MaPattern<true, 2, 0, 0, 1>;        // 2 A (+M) <=> B
+constexpr int kTpPatterns = 3;
 
 // acc * v^p for a compile-time p (0, 1 or 2), rounded products
 template <int P>
