@@ -1002,6 +1002,24 @@ def run_gpu(args):
                        "in place (hostmem.empty)" % type(kobj).__name__}
         e2e.update(hm.placement_info(hout))
         kobj.close()
+        # the host link alone: the same bytes device -> these host arrays,
+        # copied from one device buffer in 4 GiB pieces (untimed by the line)
+        import torch
+        dbuf = torch.empty(min(hout.size, 1 << 29), dtype=torch.float64, device=dev)
+        hv = torch.from_numpy(hout)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for o in range(0, hout.size, dbuf.numel()):
+            m = min(dbuf.numel(), hout.size - o)
+            hv[o:o + m].copy_(dbuf[:m], non_blocking=True)
+        torch.cuda.synchronize()
+        t_link = time.perf_counter() - t0
+        del dbuf, hv
+        e2e["link"] = {"d2h_gbs": hout.nbytes / t_link / 1e9,
+                       "d2h_floor_ms_per_step": t_link * 1e3,
+                       "fastest_call_over_floor": min(calls) / t_link,
+                       "what": "the step's output bytes copied device -> the same page-locked "
+                               "host array alone, in 4 GiB pieces: the host link's floor"}
         del hout, hphi, hP
 
     single = world == 1 and rank == 0

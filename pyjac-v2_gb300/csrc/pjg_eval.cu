@@ -360,16 +360,27 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
                 }
                 double nsacc = 0.0;
                 if (hasns) nsacc = gns * ci_;
-                if (thd) {
-                    const double wx = nux(nuk, X);
-                    for (int l = 0; l < thd_cnt; ++l) {
-                        const int sl = __ldg(slots + nsp * nsp + 2 * nsp + l * nsp + ka);
-                        if (sl >= 0)
-                            atomicAdd(accs + (int64_t)sl * a.acc_ld, __ldg(a.thd_coef + thd_off + l) * wx);
-                    }
-                    if (nslist) nsacc = fma(cns, X, nsacc);
-                }
+                if (thd && nslist) nsacc = fma(cns, X, nsacc);
                 if ((hasns || (thd && nslist)) && !a.jac_approx) accum(nsrow, k, nux(nuk, nsacc));
+            }
+            // third-body list columns: coefficient x X formed once per list
+            // entry, then +-it (or twice it) into every row of the reaction
+            // (each entry still takes this reaction's terms after its
+            // species-column terms, the order of the rows' own loops)
+            if (thd) {
+                double* accs = a.acc + s;
+                for (int l = 0; l < thd_cnt; ++l) {
+                    const double cw = __ldg(a.thd_coef + thd_off + l) * X;
+#pragma unroll
+                    for (int ka = 0; ka < PJG_MAXSP; ++ka) {
+                        if (ka >= nsp) break;
+                        if (ent_spec(ent[ka]) == last) continue;
+                        const int nuk = ST::nur(h, ka) - ST::nuf(h, ka);
+                        if (nuk == 0) continue;
+                        const int sl = __ldg(slots + nsp * nsp + 2 * nsp + l * nsp + ka);
+                        if (sl >= 0) atomicAdd(accs + (int64_t)sl * a.acc_ld, nux(nuk, cw));
+                    }
+                }
             }
         }
     };
