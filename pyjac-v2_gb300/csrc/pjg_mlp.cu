@@ -57,7 +57,17 @@ struct RowsArgs {
 // logistic sigmoid with the fast division intrinsic (2 ulp in FP32; results are
 // rounded to BF16), shared by every kernel so that training and inference
 // evaluate SiLU identically
-__device__ __forceinline__ float sigmoidf_(float x) { return __fdividef(1.0f, 1.0f + __expf(-x)); }
+// sigmoid(x) = (1 + tanh(x / 2)) / 2 with the hardware tanh (tanh.approx.f32,
+// relative error about 2^-11, below the BF16 rounding the activations take):
+// one special-function operation instead of an exponential and a reciprocal,
+// which bound the epilogues (16 special-function results per clock per SM)
+__device__ __forceinline__ float tanh_approx(float x)
+{
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float sigmoidf_(float x) { return fmaf(0.5f, tanh_approx(0.5f * x), 0.5f); }
 
 __global__ void __launch_bounds__(128, 1) umma_rows_kernel(const RowsArgs g)
 {
@@ -272,7 +282,8 @@ __global__ void __launch_bounds__(128, 1) umma_wgrad_kernel(const WgradArgs g)
 // each 128-row half of W1..W3, W4) is pre-packed in the no-swizzle core-matrix
 // layout, so one 1-D bulk copy moves it, completing on the slot's mbarrier.
 // Thread 0 issues the copies and the MMAs; the copies of the next layer's
-// weights run while the four warps read the accumulator from TMEM.
+// weights run while 16 warps (four per TMEM lane quarter, each a quarter of
+// the columns) read the accumulator from TMEM and apply bias and SiLU.
 struct FusedArgs {
     const bf16* X;       // [M x 64] features
     int64_t ldx, M;
@@ -295,7 +306,7 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b)
 // SiLU of the fused inference epilogue, the same expression as the layer kernels'
 __device__ __forceinline__ float silu_fast(float x) { return x * sigmoidf_(x); }
 
-constexpr int FUSED_THREADS = 256;  // 8 warps: two per TMEM lane quarter, each half the columns
+constexpr int FUSED_THREADS = 512;  // 16 warps: four per TMEM lane quarter, each a quarter of the columns
 
 __global__ void __launch_bounds__(FUSED_THREADS, 1) mlp_fused_kernel(const FusedArgs g)
 {
@@ -306,7 +317,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) mlp_fused_kernel(const Fused
     __shared__ int s_abort;
     __shared__ float sbias[4 * 256 + 64];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int quarter = warp & 3, half = warp >> 2;  // TMEM lanes 32 * quarter.., column half
+    const int quarter = warp & 3, part = warp >> 2;  // TMEM lanes 32 * quarter.., column quarter
     uint8_t* sA = smem;
     uint8_t* sW[2] = {smem + FUSED_SLOT, smem + 2 * FUSED_SLOT};
     if (warp == 0) {
@@ -417,7 +428,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) mlp_fused_kernel(const Fused
             const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16);
             if (l < 4) {
                 const float* bias = sbias + 256 * l;
-                for (int c0 = 128 * half; c0 < 128 * half + 128; c0 += 32) {
+                for (int c0 = 64 * part; c0 < 64 * part + 64; c0 += 32) {
                     float v[32];
                     umma::tmem_ld32(trow + (uint32_t)c0, v);
 #pragma unroll
@@ -432,9 +443,9 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) mlp_fused_kernel(const Fused
                             make_uint4(w[0], w[1], w[2], w[3]);
                     }
                 }
-            } else {
+            } else if (part < 2) {
                 const float* bias = sbias + 1024;
-                const int c0 = 32 * half;
+                const int c0 = 32 * part;
                 float v[32];
                 umma::tmem_ld32(trow + (uint32_t)c0, v);
                 if (grow < g.M) {
