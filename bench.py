@@ -1092,7 +1092,7 @@ def parse_args(argv=None):
     ap.add_argument("--implicit-large-states", type=int, default=4096,
                     help="states of the synthetic-500 Newton-matrix block (0: skip it)")
     ap.add_argument("--sur-train", type=int, default=1 << 22)
-    ap.add_argument("--sur-epochs", type=int, default=12)
+    ap.add_argument("--sur-epochs", type=int, default=60)
     ap.add_argument("--sur-eval", type=int, default=1 << 22)
     ap.add_argument("--surrogate-study", action="store_true",
                     help="only the surrogate's capacity study (depth x epochs x training states); "

@@ -37,6 +37,14 @@ int pjg_math_exp(const double* x, double* y, int64_t n, void* stream);
  * pjg_jacobian): larger problems run as several launches of this size, the
  * last one shorter.  Lets a checker sample the states at launch boundaries. */
 struct pjg_mech;
+struct pjg_tables;
+/* The reaction order of the device tables, computed on the host without a
+ * device: for packed position p, orig[p] is the mechanism's reaction index
+ * and cls[p] the code that evaluates it (0 the elementary class
+ * A + B <=> C + D, 1..10 the mass-action patterns, 11..13 the third-body and
+ * fall-off patterns, -1 the general code).  orig and cls hold tables->nr
+ * entries each. */
+int pjg_reaction_order(const struct pjg_tables* tables, int32_t* orig, int32_t* cls);
 int pjg_eval_chunk(struct pjg_mech* mech, int kind, int64_t n, char order, int jac_format,
                    int64_t* states);
 

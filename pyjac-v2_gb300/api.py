@@ -41,6 +41,41 @@ def _order(order):
     return order.encode()
 
 
+def _tables_struct(pk):
+    """The pjg_tables struct over a PackedTables' arrays (which must outlive it)."""
+    t = _lib.PjgTables()
+    t.ns, t.nr, t.flags = pk.ns, pk.nr, pk.flags
+    t.rxn = pk.rxn.ctypes.data
+    t.species = pk.species.ctypes.data_as(_lib._DP)
+    t.thd_spec = pk.thd_spec.ctypes.data_as(_lib._I32P)
+    t.thd_coef = pk.thd_coef.ctypes.data_as(_lib._DP)
+    t.n_thd = pk.n_thd
+    t.aux = pk.aux.ctypes.data_as(_lib._DP)
+    t.n_aux = pk.n_aux
+    t.nnz = pk.nnz
+    t.crs_row_ptr = pk.crs_row_ptr.ctypes.data_as(_lib._I32P)
+    t.crs_col_ind = pk.crs_col_ind.ctypes.data_as(_lib._I32P)
+    t.ccs_col_ptr = pk.ccs_col_ptr.ctypes.data_as(_lib._I32P)
+    t.ccs_row_ind = pk.ccs_row_ind.ctypes.data_as(_lib._I32P)
+    return t
+
+
+def reaction_order(mech):
+    """The order in which the device tables hold the mechanism's reactions,
+    computed on the host (pjg_reaction_order, no device needed): arrays
+    (orig, cls) with orig[p] the mechanism index of packed record p and cls[p]
+    the code that evaluates it (0 the elementary class A + B <=> C + D, 1..10
+    the mass-action patterns, 11..13 the third-body and fall-off patterns, -1
+    the general code)."""
+    pk = PackedTables(mech)
+    t = _tables_struct(pk)
+    orig = np.zeros(pk.nr, dtype=np.int32)
+    cls = np.zeros(pk.nr, dtype=np.int32)
+    _lib.check("pjg_reaction_order", _lib.load().pjg_reaction_order(
+        ctypes.byref(t), orig.ctypes.data_as(_lib._I32P), cls.ctypes.data_as(_lib._I32P)))
+    return orig, cls
+
+
 class DeviceMechanism(object):
     """Mechanism tables uploaded to the current CUDA device (owns a pjg_mech)."""
 
@@ -48,20 +83,7 @@ class DeviceMechanism(object):
         lib = _lib.load()
         self.mech = mech
         self.packed = pk = PackedTables(mech)
-        t = _lib.PjgTables()
-        t.ns, t.nr, t.flags = pk.ns, pk.nr, pk.flags
-        t.rxn = pk.rxn.ctypes.data
-        t.species = pk.species.ctypes.data_as(_lib._DP)
-        t.thd_spec = pk.thd_spec.ctypes.data_as(_lib._I32P)
-        t.thd_coef = pk.thd_coef.ctypes.data_as(_lib._DP)
-        t.n_thd = pk.n_thd
-        t.aux = pk.aux.ctypes.data_as(_lib._DP)
-        t.n_aux = pk.n_aux
-        t.nnz = pk.nnz
-        t.crs_row_ptr = pk.crs_row_ptr.ctypes.data_as(_lib._I32P)
-        t.crs_col_ind = pk.crs_col_ind.ctypes.data_as(_lib._I32P)
-        t.ccs_col_ptr = pk.ccs_col_ptr.ctypes.data_as(_lib._I32P)
-        t.ccs_row_ind = pk.ccs_row_ind.ctypes.data_as(_lib._I32P)
+        t = _tables_struct(pk)
         h = ctypes.c_void_p()
         _lib.check("pjg_mech_create", lib.pjg_mech_create(ctypes.byref(t), ctypes.byref(h)))
         self.handle = h

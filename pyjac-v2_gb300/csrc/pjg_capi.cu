@@ -86,7 +86,7 @@ extern "C" int pjg_internal_lu_solve_sparse(const void* p, int64_t n, char order
 struct pjg_mech {
     int ns = 0, nr = 0, nn = 0, need_logP = 0, nnz = 0, jac_approx = 0;
     int nr_e22 = 0;  // leading reactions of the class A + B <=> C + D
-    int ma_off[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // then the mass-action patterns (EvalArgs)
+    int ma_off[11] = {};                          // then the mass-action patterns (EvalArgs)
     int tp_off[4] = {0, 0, 0, 0};                 // then the third-body patterns (EvalArgs)
     int device = 0;
     PjgRxn* rxn = nullptr;
@@ -450,7 +450,7 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
 
 // A reaction of the class A + B <=> C + D: four distinct species with unit
 // coefficients, reversible, an Arrhenius rate form, no third body, and
-// (P_atm / R)^nu_sum = 1 (nu_sum = 0).  241 of GRI-Mech 3.0's 325 reactions.
+// (P_atm / R)^nu_sum = 1 (nu_sum = 0).  232 of GRI-Mech 3.0's 325 reactions.
 bool is_e22(const PjgRxn& R)
 {
     if (R.nspec != 4 || RX_FORM(R.flags) > FORM_ARR || !(R.flags & RX_REV) ||
@@ -477,20 +477,34 @@ bool ma_matches(const std::vector<std::pair<int, int>>& key, bool rev)
     return true;
 }
 
-// the canonical (reactant, product) coefficient list of a record: reactant
-// entries by coefficient, then product entries by coefficient; empty if a
-// species is on both sides or a coefficient is above 2
+// The canonical order of a record's entries: reactant-only entries by
+// coefficient, then entries on both sides by (reactant, product)
+// coefficients, then product-only entries by coefficient; species order kept
+// among equal coefficients.  Coefficients above 2 have no canonical order.
+bool canonical_order(const PjgRxn& R, int* idx)
+{
+    int k = 0;
+    for (int pass = 0; pass < 3; ++pass)
+        for (int a = 1; a <= 2; ++a)
+            for (int b = pass == 1 ? 1 : 0; b <= (pass == 1 ? 2 : 0); ++b)
+                for (int e = 0; e < R.nspec; ++e) {
+                    const int f = ent_nuf(R.ent[e]), r = ent_nur(R.ent[e]);
+                    if ((pass == 0 && f == a && r == 0) || (pass == 1 && f == a && r == b) ||
+                        (pass == 2 && f == 0 && r == a))
+                        idx[k++] = e;
+                }
+    return k == R.nspec;
+}
+
+// the canonical (reactant, product) coefficient list of a record; empty if a
+// coefficient is above 2
 std::vector<std::pair<int, int>> pattern_key(const PjgRxn& R)
 {
     std::vector<std::pair<int, int>> key;
-    for (int side = 0; side < 2; ++side)
-        for (int nu = 1; nu <= 2; ++nu)
-            for (int e = 0; e < R.nspec; ++e) {
-                const int f = ent_nuf(R.ent[e]), r = ent_nur(R.ent[e]);
-                if (side == 0 && f == nu && r == 0) key.push_back({f, 0});
-                if (side == 1 && r == nu && f == 0) key.push_back({0, r});
-            }
-    if ((int)key.size() != R.nspec) key.clear();
+    int idx[PJG_MAXSP];
+    if (!canonical_order(R, idx)) return key;
+    for (int k = 0; k < R.nspec; ++k)
+        key.push_back({ent_nuf(R.ent[idx[k]]), ent_nur(R.ent[idx[k]])});
     return key;
 }
 
@@ -507,30 +521,26 @@ int tp_pattern_of(const PjgRxn& R)
     return -1;
 }
 
-// the record with its entries in the canonical order of pattern_key
+// the record with its entries in the canonical order (a pattern's record)
 PjgRxn canonical_entries(const PjgRxn& R)
 {
     PjgRxn c = R;
-    int k = 0;
-    for (int side = 0; side < 2; ++side)
-        for (int nu = 1; nu <= 2; ++nu)
-            for (int e = 0; e < R.nspec; ++e)
-                if ((side == 0 ? ent_nuf(R.ent[e]) : ent_nur(R.ent[e])) == nu &&
-                    (side == 0 ? ent_nur(R.ent[e]) : ent_nuf(R.ent[e])) == 0)
-                    c.ent[k++] = R.ent[e];
+    int idx[PJG_MAXSP];
+    if (canonical_order(R, idx))
+        for (int k = 0; k < R.nspec; ++k) c.ent[k] = R.ent[idx[k]];
     return c;
 }
 
-// MaP0..MaP7: reactions without third body, of an Arrhenius form, whose
-// canonical coefficient list matches a pattern; -1 otherwise (entries on both
-// sides, coefficients above 2, third bodies, fall-off, PLOG and Chebyshev
-// keep the general code)
+// MaP0..MaP9: reactions without third body, of an Arrhenius form, whose
+// canonical coefficient list matches a pattern; -1 otherwise (other shapes,
+// coefficients above 2, third bodies, fall-off, PLOG and Chebyshev keep the
+// general code)
 int ma_pattern_of(const PjgRxn& R)
 {
     if (RX_FORM(R.flags) > FORM_ARR || RX_THD(R.flags) != THD_NONE || R.nspec < 3 || R.nspec > 5)
         return -1;
     const auto key = pattern_key(R);
-    if (key.empty()) return -1;  // a species on both sides, or a coefficient > 2
+    if (key.empty()) return -1;  // a coefficient > 2
     const bool rev = R.flags & RX_REV;
     if (ma_matches<pjg::MaP0>(key, rev)) return 0;
     if (ma_matches<pjg::MaP1>(key, rev)) return 1;
@@ -540,60 +550,81 @@ int ma_pattern_of(const PjgRxn& R)
     if (ma_matches<pjg::MaP5>(key, rev)) return 5;
     if (ma_matches<pjg::MaP6>(key, rev)) return 6;
     if (ma_matches<pjg::MaP7>(key, rev)) return 7;
+    if (ma_matches<pjg::MaP8>(key, rev)) return 8;
+    if (ma_matches<pjg::MaP9>(key, rev)) return 9;
     return -1;
 }
 
-// Reactions of the class above go first, each with its entries reordered
-// reactants first (species order kept within each side), so that the kernels
-// evaluate them by straight-line code with coefficients known at compile
-// time; the others follow in mechanism order.  Nothing outside the kernels
-// depends on the reaction order: the species rates and the Jacobian are sums
-// over reactions, and the slot tables are built from these records.
-void order_reactions(pjg_mech* m)
+// The packed reaction order of the device tables: the class above first,
+// each with its entries reordered reactants first (species order kept within
+// each side); then the mass-action patterns MaP0..MaP9 and the third-body
+// patterns TpP0..TpP2 (pjg_rxn.cuh), each reaction with its entries in the
+// pattern's order (canonical_entries); then the rest in mechanism order.
+// The kernels evaluate each group by code compiled for it.  Nothing outside
+// the kernels depends on the reaction order: the species rates and the
+// Jacobian are sums over reactions, and the slot tables are built from these
+// records.  orig[p] is the mechanism index of packed record p, cls[p] its
+// group: 0 the elementary class, 1 + q pattern MaPq, 1 + kMaPatterns + t
+// pattern TpPt, -1 the general code.
+struct Packing {
+    std::vector<PjgRxn> rx;
+    std::vector<int> orig, cls;
+    int nr_e22 = 0;
+    int ma_off[pjg::kMaPatterns + 1] = {};
+    int tp_off[pjg::kTpPatterns + 1] = {};
+};
+
+void pack_reactions(const std::vector<PjgRxn>& in, Packing& pk)
 {
-    std::vector<PjgRxn> head, tail;
-    for (const PjgRxn& R : m->h_rxn) {
-        if (!is_e22(R)) {
-            tail.push_back(R);
-            continue;
+    const int nma = pjg::kMaPatterns, ntp = pjg::kTpPatterns;
+    std::vector<std::vector<int>> groups(1 + nma + ntp + 1);  // indices into `in`
+    for (int i = 0; i < (int)in.size(); ++i) {
+        const PjgRxn& R = in[i];
+        int g;
+        if (is_e22(R)) {
+            g = 0;
+        } else {
+            const int q = ma_pattern_of(R), t = q < 0 ? tp_pattern_of(R) : -1;
+            g = q >= 0 ? 1 + q : t >= 0 ? 1 + nma + t : 1 + nma + ntp;
         }
-        PjgRxn c = R;
-        int q = 0;
-        for (int side = 0; side < 2; ++side)
-            for (int e = 0; e < 4; ++e)
-                if ((ent_nuf(R.ent[e]) == 1) == (side == 0)) c.ent[q++] = R.ent[e];
-        head.push_back(c);
+        groups[g].push_back(i);
     }
-    m->nr_e22 = (int)head.size();
-    // then the mass-action patterns MaP0..MaP7 (pjg_rxn.cuh), entries in the
-    // pattern's order: reactants by coefficient, then products by
-    // coefficient (species order kept among equal coefficients)
-    // then the third-body patterns TpP0..TpP2, the same entry order
-    std::vector<PjgRxn> rest;
-    std::vector<std::vector<PjgRxn>> byp(pjg::kMaPatterns), byt(pjg::kTpPatterns);
-    for (const PjgRxn& R : tail) {
-        const int q = ma_pattern_of(R), t = q < 0 ? tp_pattern_of(R) : -1;
-        if (q >= 0) byp[q].push_back(canonical_entries(R));
-        else if (t >= 0) byt[t].push_back(canonical_entries(R));
-        else rest.push_back(R);
+    pk.rx.clear();
+    pk.orig.clear();
+    pk.cls.clear();
+    for (int g = 0; g < (int)groups.size(); ++g) {
+        if (g >= 1 && g <= nma) pk.ma_off[g - 1] = (int)pk.rx.size();
+        if (g > nma && g <= nma + ntp) pk.tp_off[g - 1 - nma] = (int)pk.rx.size();
+        for (int i : groups[g]) {
+            const PjgRxn& R = in[i];
+            PjgRxn c = R;
+            if (g == 0) {
+                int q = 0;
+                for (int side = 0; side < 2; ++side)
+                    for (int e = 0; e < 4; ++e)
+                        if ((ent_nuf(R.ent[e]) == 1) == (side == 0)) c.ent[q++] = R.ent[e];
+            } else if (g <= nma + ntp) {
+                c = canonical_entries(R);
+            }
+            pk.rx.push_back(c);
+            pk.orig.push_back(i);
+            pk.cls.push_back(g <= nma + ntp ? g : -1);
+        }
+        if (g == 0) pk.nr_e22 = (int)pk.rx.size();
+        if (g == nma) pk.ma_off[nma] = (int)pk.rx.size();
+        if (g == nma + ntp) pk.tp_off[ntp] = (int)pk.rx.size();
     }
-    int pos = m->nr_e22;
-    for (int q = 0; q < pjg::kMaPatterns; ++q) {
-        m->ma_off[q] = pos;
-        head.insert(head.end(), byp[q].begin(), byp[q].end());
-        pos += (int)byp[q].size();
-    }
-    m->ma_off[pjg::kMaPatterns] = pos;
-    for (int q = 0; q < pjg::kTpPatterns; ++q) {
-        m->tp_off[q] = pos;
-        head.insert(head.end(), byt[q].begin(), byt[q].end());
-        pos += (int)byt[q].size();
-    }
-    m->tp_off[pjg::kTpPatterns] = pos;
-    head.insert(head.end(), rest.begin(), rest.end());
-    m->h_rxn.swap(head);
 }
 
+void order_reactions(pjg_mech* m)
+{
+    Packing pk;
+    pack_reactions(m->h_rxn, pk);
+    m->h_rxn.swap(pk.rx);
+    m->nr_e22 = pk.nr_e22;
+    for (int q = 0; q <= pjg::kMaPatterns; ++q) m->ma_off[q] = pk.ma_off[q];
+    for (int q = 0; q <= pjg::kTpPatterns; ++q) m->tp_off[q] = pk.tp_off[q];
+}
 
 }  // namespace
 
@@ -880,6 +911,23 @@ int pjg_mech_destroy(pjg_mech* m)
         cudaFree(t.cj_slots);
     }
     delete m;
+    return 0;
+}
+
+int pjg_reaction_order(const pjg_tables* tb, int32_t* orig, int32_t* cls)
+{
+    if (!tb || tb->nr < 0 || (tb->nr > 0 && (!tb->rxn || !orig || !cls)))
+        return fail(PJG_ERR_ARG, "invalid tables or null output");
+    const PjgRxn* r = (const PjgRxn*)tb->rxn;
+    for (int i = 0; i < tb->nr; ++i)
+        if (r[i].nspec < 1 || r[i].nspec > PJG_MAXSP)
+            return fail(PJG_ERR_TABLES, "reaction record out of range");
+    Packing pk;
+    pack_reactions(std::vector<PjgRxn>(r, r + tb->nr), pk);
+    for (int p = 0; p < tb->nr; ++p) {
+        orig[p] = pk.orig[p];
+        cls[p] = pk.cls[p];
+    }
     return 0;
 }
 

@@ -171,11 +171,23 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     }
 
     // ------------------------------------- reactions A + B <=> C + D (packed first)
+    // the next reaction's record and per-state values are loaded while this
+    // one computes
+    E22Head hn;
+    E22Vals vn;
+    if (a.nr_e22 > 0) {
+        load_e22(a.rxn, hn);
+        e22_fetch<DER>(hn, conc, bk, db, vn);
+    }
     for (int i = 0; i < a.nr_e22; ++i) {
-        E22Head h;
-        load_e22(a.rxn + i, h);
+        const E22Head h = hn;
+        const E22Vals vv = vn;
+        if (i + 1 < a.nr_e22) {
+            load_e22(a.rxn + i + 1, hn);
+            e22_fetch<DER>(hn, conc, bk, db, vn);
+        }
         E22Terms o;
-        e22_terms<DER>(h, last, sv, conc, bk, db, o);
+        e22_terms_v<DER>(h, vv, last, sv, o);
         accum(wdot, h.s[0], -o.net);
         accum(wdot, h.s[1], -o.net);
         accum(wdot, h.s[2], o.net);
@@ -227,7 +239,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
 #pragma unroll
             for (int e = 0; e < N; ++e) {
                 sp[e] = ent_spec(h.ent[e]);
-                accum(wdot, sp[e], nux(PT::nur(e) - PT::nuf(e), o.net));
+                if (PT::nur(e) != PT::nuf(e)) accum(wdot, sp[e], nux(PT::nur(e) - PT::nuf(e), o.net));
             }
             if (!DER) continue;
             const bool hasns = (h.flags & RX_HASNS) && !a.jac_approx;
@@ -251,7 +263,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
 #pragma unroll
             for (int ka = 0; ka < N; ++ka) {
                 const int nuk = PT::nur(ka) - PT::nuf(ka);
-                if (sp[ka] == last) continue;
+                if (nuk == 0 || sp[ka] == last) continue;
 #pragma unroll
                 for (int jb = 0; jb < N + 2; ++jb) {
                     const int sl = jb < N ? __ldg(slots + ka * N + jb)
@@ -271,6 +283,8 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     ma_range(MaP5{}, a.ma_off[5], a.ma_off[6]);
     ma_range(MaP6{}, a.ma_off[6], a.ma_off[7]);
     ma_range(MaP7{}, a.ma_off[7], a.ma_off[8]);
+    ma_range(MaP8{}, a.ma_off[8], a.ma_off[9]);
+    ma_range(MaP9{}, a.ma_off[9], a.ma_off[10]);
 
     // ------------------------------------------------------- other reactions
     // (the general code; third-body and fall-off reactions of the patterns

@@ -30,10 +30,10 @@ struct EvalArgs {
     const double* aux;
     int ns, nr;
     int nr_e22;      // reactions [0, nr_e22) are of the class A + B <=> C + D (see pjg_rxn.cuh)
-    int ma_off[9];   // then [ma_off[q], ma_off[q + 1]) of mass-action pattern q (MaP0..MaP7),
+    int ma_off[11];  // then [ma_off[q], ma_off[q + 1]) of mass-action pattern q (MaP0..MaP9),
                      // ma_off[0] = nr_e22
     int tp_off[4];   // then [tp_off[q], tp_off[q + 1]) of third-body pattern q (TpP0..TpP2),
-                     // tp_off[0] = ma_off[8]; the others from tp_off[3]
+                     // tp_off[0] = ma_off[10]; the others from tp_off[3]
     int need_logP;
     int jac_approx;  // 'approximate' Jacobian type: no bath-gas terms in the species columns
     // states

@@ -408,21 +408,37 @@ struct E22Terms {
     double d0, d1;
 };
 
+// the per-state values one elementary reaction reads (loaded ahead of use)
+struct E22Vals {
+    double c[4], b[4], db[4];
+};
+
 template <bool DER, class ARR>
-__device__ __forceinline__ void e22_terms(const E22Head& h, int last, const StateVars& sv,
-                                          const ARR& conc, const ARR& bk, const ARR& db,
-                                          E22Terms& o)
+__device__ __forceinline__ void e22_fetch(const E22Head& h, const ARR& conc, const ARR& bk,
+                                          const ARR& db, E22Vals& v)
+{
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        v.c[q] = conc[h.s[q]];
+        v.b[q] = bk[h.s[q]];
+        if (DER) v.db[q] = db[h.s[q]];
+    }
+}
+
+template <bool DER>
+__device__ __forceinline__ void e22_terms_v(const E22Head& h, const E22Vals& vv, int last,
+                                            const StateVars& sv, E22Terms& o)
 {
     const double* p = h.p;
     const double b = ldg(p + P_B), Ta = ldg(p + P_TA);
     const double kf = arrhenius(RX_FORM(h.flags), ldg(p + P_A), b, Ta, h.bint, sv.Tc, sv.logT,
                                 sv.Tinv, sv.etab);
-    double Bsum = 0.0 - bk[h.s[0]];
-    Bsum = Bsum - bk[h.s[1]];
-    Bsum = Bsum + bk[h.s[2]];
-    Bsum = Bsum + bk[h.s[3]];
+    double Bsum = 0.0 - vv.b[0];
+    Bsum = Bsum - vv.b[1];
+    Bsum = Bsum + vv.b[2];
+    Bsum = Bsum + vv.b[3];
     const double kr = kf * fexp(-fmin(EXP_MAX, Bsum), sv.etab);
-    const double c0 = conc[h.s[0]], c1 = conc[h.s[1]], c2 = conc[h.s[2]], c3 = conc[h.s[3]];
+    const double c0 = vv.c[0], c1 = vv.c[1], c2 = vv.c[2], c3 = vv.c[3];
     // rounded products and difference (no contraction into an FMA): the rate
     // of progress must be the same in every kernel kind, whatever else uses
     // rf and rr (the Jacobian's rates equal the rates kernel's bit for bit)
@@ -430,10 +446,10 @@ __device__ __forceinline__ void e22_terms(const E22Head& h, int last, const Stat
     o.net = __dsub_rn(rf, rr);
     if (!DER) return;
     const double dlnkf_dT = (b + Ta * sv.Tjinv) * sv.Tjinv;
-    double dB = 0.0 - db[h.s[0]];
-    dB = dB - db[h.s[1]];
-    dB = dB + db[h.s[2]];
-    dB = dB + db[h.s[3]];
+    double dB = 0.0 - vv.db[0];
+    dB = dB - vv.db[1];
+    dB = dB + vv.db[2];
+    dB = dB + vv.db[3];
     o.g[0] = kf * gsmall(c1);
     o.g[1] = kf * gsmall(c0);
     o.g[2] = -(kr * gsmall(c3));
@@ -458,7 +474,8 @@ __device__ __forceinline__ void e22_terms(const E22Head& h, int last, const Stat
 // Other mass-action reactions without a third body, in a few fixed
 // stoichiometric patterns (MaPattern below; pjg_capi.cu order_reactions packs
 // each pattern's reactions together, entries in the pattern's order:
-// reactants by coefficient, then products by coefficient).  The arithmetic
+// reactants by coefficient, then species on both sides, then products by
+// coefficient).  The arithmetic
 // of rxn_terms() for such a reaction with every coefficient known at compile
 // time.  Up to five entries.
 template <bool REV, int F0, int R0, int F1, int R1, int F2 = 0, int R2 = 0, int F3 = 0, int R3 = 0,
@@ -487,7 +504,9 @@ using MaP4 = MaPattern<true, 1, 0, 1, 0, 1, 0, 0, 1, 0, 1>;   // A + B + C <=> D
 using MaP5 = MaPattern<true, 1, 0, 1, 0, 0, 1, 0, 2>;         // A + B <=> C + 2 D
 using MaP6 = MaPattern<true, 1, 0, 2, 0, 0, 1, 0, 1>;         // A + 2 B <=> C + D
 using MaP7 = MaPattern<false, 1, 0, 1, 0, 0, 1, 0, 1>;        // A + B => C + D
-constexpr int kMaPatterns = 8;
+using MaP8 = MaPattern<true, 1, 0, 1, 1, 0, 1>;               // A + X <=> B + X
+using MaP9 = MaPattern<true, 1, 0, 1, 0, 1, 1, 0, 1>;         // A + B + X <=> C + X
+constexpr int kMaPatterns = 10;
 
 // coefficient patterns of reactions with a third body or fall-off, evaluated
 // by the general code (rxn_terms) compiled per pattern (PatStoich)

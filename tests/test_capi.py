@@ -41,7 +41,7 @@ def test_instrumentation_hooks_are_not_in_the_boundary_header():
     public = set(declared_functions(("pyjac_gb300.h",)))
     internal = set(declared_functions(("pyjac_gb300_internal.h",)))
     assert internal == {"pjg_launch_count", "pjg_fp64_peak", "pjg_profile_begin",
-                        "pjg_profile_end", "pjg_math_exp", "pjg_eval_chunk"}
+                        "pjg_profile_end", "pjg_math_exp", "pjg_eval_chunk", "pjg_reaction_order"}
     assert not public & internal
 
 

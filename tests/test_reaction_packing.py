@@ -1,0 +1,88 @@
+"""The packed reaction order of the device tables (host logic, no GPU).
+
+The evaluation kernels run reactions in groups, each compiled for its
+stoichiometry: the elementary class A + B <=> C + D, eight mass-action
+patterns without third body and three third-body / fall-off patterns, then
+the general code for the rest.  pjg_reaction_order returns the library's
+packing; here it is checked against a plain restatement of the rules on the
+packed records of the mechanism: every reaction appears once, each group
+holds exactly the reactions the rules assign to it, in mechanism order, and
+the groups come in the order the kernels run them.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_mech, pkg
+
+# (reversible, canonical coefficients): reactant entries by coefficient,
+# then entries on both sides, then product entries by coefficient
+MA = [(False, [(1, 0), (1, 0), (0, 1), (0, 1), (0, 1)]),
+      (True, [(1, 0), (1, 0), (0, 1), (0, 1), (0, 1)]),
+      (True, [(1, 0), (1, 0), (0, 2)]),
+      (True, [(2, 0), (0, 1), (0, 1)]),
+      (True, [(1, 0), (1, 0), (1, 0), (0, 1), (0, 1)]),
+      (True, [(1, 0), (1, 0), (0, 1), (0, 2)]),
+      (True, [(1, 0), (2, 0), (0, 1), (0, 1)]),
+      (False, [(1, 0), (1, 0), (0, 1), (0, 1)]),
+      (True, [(1, 0), (1, 1), (0, 1)]),
+      (True, [(1, 0), (1, 0), (1, 1), (0, 1)])]
+TP = [(True, [(1, 0), (1, 0), (0, 1)]),
+      (True, [(1, 0), (0, 1), (0, 1)]),
+      (True, [(2, 0), (0, 1)])]
+
+
+def _key(rec):
+    """Reactant-only entries by coefficient, then entries on both sides, then
+    product-only entries by coefficient; None with a coefficient above 2."""
+    ents = [(int(e >> 16) & 0xFF, int(e >> 24)) for e in rec["ent"][:rec["nspec"]]]
+    if any(max(f, r) > 2 for f, r in ents):
+        return None
+    return (sorted(x for x in ents if x[1] == 0) + sorted(x for x in ents if x[0] and x[1]) +
+            sorted(x for x in ents if x[0] == 0))
+
+
+def expected_class(rec):
+    flags = int(rec["flags"])
+    form, rev, thd = flags & 7, bool(flags & 8), (flags >> 4) & 3
+    key = _key(rec)
+    if form > 2 or key is None:
+        return -1
+    if (rec["nspec"] == 4 and rev and thd == 0 and rec["nu_sum"] == 0 and rec["p"][11] == 1.0
+            and key == [(1, 0), (1, 0), (0, 1), (0, 1)]):
+        return 0
+    if thd == 0 and 3 <= rec["nspec"] <= 5:
+        for q, (r, k) in enumerate(MA):
+            if r == rev and k == key:
+                return 1 + q
+    if thd != 0:
+        for t, (r, k) in enumerate(TP):
+            if r == rev and k == key:
+                return 1 + len(MA) + t
+    return -1
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30", "testmech", "synthetic_small"])
+def test_packing_matches_the_rules(name):
+    mech = load_mech(name)
+    orig, cls = pkg("api").reaction_order(mech)
+    rx = pkg("pack").PackedTables(mech).rxn
+    assert sorted(orig.tolist()) == list(range(len(rx)))
+    want = np.array([expected_class(rx[i]) for i in orig])
+    assert np.array_equal(cls, want)
+    # groups in kernel order (elementary, patterns, general last), each in
+    # mechanism order
+    rank = np.where(cls < 0, 99, cls)
+    assert np.all(np.diff(rank) >= 0)
+    for g in np.unique(rank):
+        assert np.all(np.diff(orig[rank == g]) > 0)
+
+
+def test_gri30_group_sizes():
+    """GRI-Mech 3.0: 232 elementary reactions, 41 in the mass-action patterns,
+    all 41 third-body and fall-off reactions in the third-body patterns, 11
+    for the general code."""
+    orig, cls = pkg("api").reaction_order(load_mech("gri30"))
+    assert int((cls == 0).sum()) == 232
+    assert int(((cls >= 1) & (cls <= 10)).sum()) == 41
+    assert int(((cls >= 11) & (cls <= 13)).sum()) == 41
+    assert int((cls == -1).sum()) == 11
