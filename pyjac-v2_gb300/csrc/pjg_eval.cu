@@ -115,13 +115,13 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     // concentrations (rate_subs.py get_concentrations :597-706)
     double nsum = 0.0;
     for (int k = 0; k < last; ++k) {
-        const double nk = fmax(SMALL, ph[(int64_t)(2 + k) * a.phi_sj]);
+        const double nk = gsmall(ph[(int64_t)(2 + k) * a.phi_sj]);
         nsum = nsum + nk;
         conc[k] = nk * Vinv;
         wdot[k] = 0.0;
         if (DER) nsrow[k] = 0.0;
     }
-    conc[last] = P / (RU * Tc) + -1.0 * fmax(SMALL, nsum) * Vinv;
+    conc[last] = P / (RU * Tc) + -1.0 * gsmall(nsum) * Vinv;
     wdot[last] = 0.0;
 
     // thermo: Gibbs functions for Kc (+ derivatives and cp, h for the Jacobian)
@@ -188,8 +188,8 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         }
         E22Terms o;
         e22_terms_v<DER>(h, vv, last, sv, o);
-        accum(wdot, h.s[0], -o.net);
-        accum(wdot, h.s[1], -o.net);
+        accum(wdot, h.s[0], negi(o.net));
+        accum(wdot, h.s[1], negi(o.net));
         accum(wdot, h.s[2], o.net);
         accum(wdot, h.s[3], o.net);
         if (!DER) continue;
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
 #pragma unroll
             for (int ka = 0; ka < 4; ++ka)
                 if (h.s[ka] != last) w = ka < 2 ? w - hw[h.s[ka]] : w + hw[h.s[ka]];
-            if (w != 0.0) {
+            if (nonzero(w)) {
 #pragma unroll
                 for (int jb = 0; jb < 4; ++jb)
                     if (h.s[jb] != last) accum(nsrow, h.s[jb], w * o.g[jb]);
@@ -220,9 +220,9 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
             for (int jb = 0; jb < 6; ++jb) {
                 const int sl = jb < 4 ? __ldg(slots + ka * 4 + jb) : __ldg(slots + 16 + 2 * ka + (jb - 4));
                 const double v = jb < 4 ? o.g[jb] : (jb == 4 ? o.d0 : o.d1);
-                if (sl >= 0) atomicAdd(accs + (int64_t)sl * a.acc_ld, ka < 2 ? -v : v);
+                if (sl >= 0) atomicAdd(accs + (int64_t)sl * a.acc_ld, ka < 2 ? negi(v) : v);
             }
-            if (hasns) accum(nsrow, k, ka < 2 ? -o.gns : o.gns);
+            if (hasns) accum(nsrow, k, ka < 2 ? negi(o.gns) : o.gns);
         }
     }
 
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
 #pragma unroll
                 for (int ka = 0; ka < N; ++ka)
                     if (sp[ka] != last) w = addnu(w, PT::nur(ka) - PT::nuf(ka), hw[sp[ka]]);
-                if (w != 0.0) {
+                if (nonzero(w)) {
 #pragma unroll
                     for (int jb = 0; jb < N; ++jb)
                         if (sp[jb] != last) accum(nsrow, sp[jb], w * o.g[jb]);
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
                     if (k == last) continue;
                     w = addnu(w, ST::nur(h, ka) - ST::nuf(h, ka), hw[k]);
                 }
-                if (w != 0.0) {
+                if (nonzero(w)) {
                     const double wc = w * ci_;
 #pragma unroll
                     for (int jb = 0; jb < PJG_MAXSP; ++jb) {
@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
                     Jv[q] = j0 + q < last ? __ldcg(rowp + (int64_t)((2 + j0 + q) * cs) * ld) : 0.0;
                 const double v = rd(nsrow, k), hwk = hw[k];
                 const double omk = ldg(a.sp + (int64_t)k * PJG_SP_DOUBLES + SP_OMW);
-                if (v != 0.0) {
+                if (nonzero(v)) {
 #pragma unroll
                     for (int q = 0; q < kCols; ++q) {
                         Jv[q] = Jv[q] - v;
@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         // column of the pattern), then the column sums of rows T and E
         for (int k = 0; k < last; ++k) {
             const double v = rd(nsrow, k);
-            if (v == 0.0) continue;
+            if (!nonzero(v)) continue;
             const int r0 = __ldg(a.row_off + k), r1 = __ldg(a.row_off + k + 1);
             for (int q = r0; q < r1; ++q) {
                 const int2 e = __ldg(a.row_list + q);

@@ -119,9 +119,22 @@ __device__ __forceinline__ double fexp(double x, const double* tab)
     return __longlong_as_double(__double_as_longlong(y) + ((long long)(n >> PJG_EXP_BITS) << 52));
 }
 
+// min(c, x) for a positive constant c on the integer pipe (GB300's FP64 pipe
+// is the kernels' bound): as signed 64-bit integers, doubles order like
+// their values against a positive c, negative values having the sign bit set.
+// Equal to fmin(c, x) for every x but a NaN with the sign bit set, which it
+// returns where fmin returns c.
+__device__ __forceinline__ double min_pos(double c, double x)
+{
+    return __double_as_longlong(x) < __double_as_longlong(c) ? x : c;
+}
+
+// x != 0.0 on the integer pipe (either zero compares equal, NaN unequal)
+__device__ __forceinline__ bool nonzero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+
 // exp(min(x, 690.775527898)), the reference's guarded exponential
 // (pyjac/core/instruction_creator.py GuardedExp :436-448)
-__device__ __forceinline__ double gexp(double x, const double* tab) { return fexp(fmin(EXP_MAX, x), tab); }
+__device__ __forceinline__ double gexp(double x, const double* tab) { return fexp(min_pos(EXP_MAX, x), tab); }
 
 // positive-argument max(1e-300, x) guard without an FP64 instruction: for
 // x >= 0 the IEEE order equals the integer order of the bit patterns, and a

@@ -24,13 +24,20 @@
 namespace pjg {
 
 // nu * x for a warp-uniform small integer nu without an int->double conversion
+// -x by flipping the sign bit on the integer pipe: a value that only feeds a
+// reduction cannot fold the negation into an FP64 instruction
+__device__ __forceinline__ double negi(double x)
+{
+    return __hiloint2double(__double2hiint(x) ^ 0x80000000, __double2loint(x));
+}
+
 __device__ __forceinline__ double nux(int nu, double x)
 {
     switch (nu) {
     case 1: return x;
-    case -1: return -x;
+    case -1: return negi(x);
     case 2: return x + x;
-    case -2: return -(x + x);
+    case -2: return negi(x + x);
     case 0: return 0.0;
     }
     return (double)nu * x;
@@ -152,7 +159,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
         kf = gexp(plog_logk(aux + h.auxo, logT, Tinv, sv.logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP), et);
     } else {
         const double l10 = cheb_log10k(aux + h.auxo, Tinv, sv.logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP);
-        kf = fexp(LN10 * fmin(EXP_MAX, l10), et);
+        kf = fexp(LN10 * min_pos(EXP_MAX, l10), et);
         dlnkf_dT *= LN10;
         dlnkf_dlnP *= LN10;
     }
@@ -169,7 +176,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                 if (DER) dB = addnu(dB, nu, db[ent_spec(h.ent[e])]);
             }
         }
-        kr = kf * ldg(p + P_PSUM) * fexp(-fmin(EXP_MAX, Bsum), et);
+        kr = kf * ldg(p + P_PSUM) * fexp(-min_pos(EXP_MAX, Bsum), et);
     }
     // rates of progress (mass action on raw concentrations)
     double rf = kf, rr = kr;
@@ -200,7 +207,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
             fs.kratio = chem ? kf / kfall : kfall / kf;  // k0 / kinf
             fs.Pr = M * fs.kratio;
             if (blend == BL_TROE) {
-                const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
+                const double logPr = log(gsmall(fs.Pr)) * INV_LN10;
                 const double ta = ldg(p + P_F0);
                 fs.e1 = gexp(-1.0 * Tc * ldg(p + P_F1), et);
                 fs.e3 = gexp(-1.0 * Tc * ldg(p + P_F3), et);
@@ -209,7 +216,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                     fs.e2 = gexp(-1.0 * ldg(p + P_F2) * Tinv, et);
                     Fc = Fc + fs.e2;
                 }
-                fs.lnFc = log(fmax(SMALL, Fc));
+                fs.lnFc = log(gsmall(Fc));
                 const double logFc = fs.lnFc * INV_LN10;
                 fs.B = -1.1762 * logFc + -0.14 * logPr + 0.806;
                 fs.A = -0.67 * logFc + logPr + -0.4;
@@ -217,7 +224,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                 const double B2 = fs.B * fs.B;
                 fs.Fi = fexp(B2 / (fs.A * fs.A + B2) * fs.lnFc, et);
             } else if (blend == BL_SRI) {
-                const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
+                const double logPr = log(gsmall(fs.Pr)) * INV_LN10;
                 fs.X = 1.0 / (logPr * logPr + 1.0);
                 fs.e1 = gexp(-ldg(p + P_F1) * Tinv, et);
                 fs.e3 = gexp(-Tc / ldg(p + P_F2), et);
@@ -286,10 +293,10 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
         if (blend == BL_TROE) {
             const double absq = fs.A * fs.A + fs.B * fs.B;
             dlnFi_dPr = -2.0 * fs.A * fs.B * fs.lnFc * (0.14 * fs.A + fs.B) /
-                        (fmax(SMALL, fs.Pr) * absq * absq * LN10);
+                        (gsmall(fs.Pr) * absq * absq * LN10);
         } else if (blend == BL_SRI) {
-            const double logPr = log(fmax(SMALL, fs.Pr)) * INV_LN10;
-            dlnFi_dPr = -2.0 * fs.X * fs.X * logPr / (fmax(SMALL, fs.Pr) * LN10) * fs.lnQ;
+            const double logPr = log(gsmall(fs.Pr)) * INV_LN10;
+            dlnFi_dPr = -2.0 * fs.X * fs.X * logPr / (gsmall(fs.Pr) * LN10) * fs.lnQ;
         }
     }
     // d ci / dx given d Pr / dx = Pr theta + theta_n and the direct part of d ln Fi / dx
@@ -437,7 +444,7 @@ __device__ __forceinline__ void e22_terms_v(const E22Head& h, const E22Vals& vv,
     Bsum = Bsum - vv.b[1];
     Bsum = Bsum + vv.b[2];
     Bsum = Bsum + vv.b[3];
-    const double kr = kf * fexp(-fmin(EXP_MAX, Bsum), sv.etab);
+    const double kr = kf * fexp(-min_pos(EXP_MAX, Bsum), sv.etab);
     const double c0 = vv.c[0], c1 = vv.c[1], c2 = vv.c[2], c3 = vv.c[3];
     // rounded products and difference (no contraction into an FMA): the rate
     // of progress must be the same in every kernel kind, whatever else uses
@@ -555,7 +562,7 @@ __device__ __forceinline__ void ma_terms(const RxnHead& h, int last, const State
             Bsum = addnu(Bsum, PT::nur(e) - PT::nuf(e), bk[sp[e]]);
             if (DER) dB = addnu(dB, PT::nur(e) - PT::nuf(e), db[sp[e]]);
         }
-        kr = kf * ldg(p + P_PSUM) * fexp(-fmin(EXP_MAX, Bsum), sv.etab);
+        kr = kf * ldg(p + P_PSUM) * fexp(-min_pos(EXP_MAX, Bsum), sv.etab);
     }
     // rounded products and difference: the rate of progress is the same in
     // every kernel kind (see e22_terms)
