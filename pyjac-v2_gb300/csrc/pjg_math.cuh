@@ -45,15 +45,17 @@ __device__ __forceinline__ double mulpow(double acc, double v, int p)
 
 // Table of 2^(j/2^B), j = 0 .. 2^B - 1, in shared memory (B = PJG_EXP_BITS):
 // every kernel that calls fexp fills one per block with fill_exp_table before
-// its first use.  B = 6 (64 entries) is the default.  Its random lookups meet
-// bank conflicts, which B = 4 (16 entries, one bank pair each) avoids and
-// B = 0 (no table) does without, both at the price of a longer polynomial.
-// Measured on GB300 (1,048,576 GRI-Mech 3.0 states, F order), B = 4 and
-// B = 0 against B = 6: the Jacobian kernel 2.6 % and 8.3 % slower, the
-// species-rate kernel 13 % and 30 % slower (40.7 and 47.0 ms against 36.1):
-// the FP64 instruction count, not the shared-memory lookups, sets the time.
+// its first use.  B = 8 (256 entries, 2 KB) is the default: its polynomial
+// has one FMA fewer than B = 6's.  The random lookups meet bank conflicts,
+// which B = 4 (16 entries, one bank pair each) avoids and B = 0 (no table)
+// does without, both at the price of a longer polynomial.  Measured on GB300
+// (1,048,576 GRI-Mech 3.0 states, F order): B = 4 and B = 0 against B = 6, the
+// Jacobian kernel 2.6 % and 8.3 % slower, the species-rate kernel 13 % and
+// 30 % slower; B = 8 against B = 6, the Jacobian 73.5 against 74.3 ms and the
+// species rates 29.0 against 30.1 ms.  The FP64 instruction count, not the
+// shared-memory lookups, sets the time.
 #ifndef PJG_EXP_BITS
-#define PJG_EXP_BITS 6
+#define PJG_EXP_BITS 8
 #endif
 #define PJG_EXP_TAB (1 << PJG_EXP_BITS)
 
@@ -67,9 +69,10 @@ __device__ __forceinline__ void fill_exp_table(double* tab)
 // implementation of the exponential function in IEEE floating-point
 // arithmetic", ACM TOMS 15(2), 1989): x = (2^B m + j) ln2 / 2^B + r with
 // |r| <= ln2 / 2^(B+1), so exp(x) = 2^m 2^(j/2^B) exp(r), and exp(r) - 1 is
-// its Taylor polynomial, of degree 5 for B = 6 (|r| <= 0.0055, truncation
-// below 4e-17 relative), 7 for B = 4 (|r| <= 0.022, below 2e-18) and 13 for
-// B = 0 (|r| <= 0.35, below 5e-18).  The reduction is Cody and Waite's with
+// its Taylor polynomial, of degree 4 for B = 8 (|r| <= 0.00136, truncation
+// below 4e-17 relative), 5 for B = 6 (|r| <= 0.0055, below 4e-17), 7 for
+// B = 4 (|r| <= 0.022, below 2e-18) and 13 for B = 0 (|r| <= 0.35, below
+// 5e-18).  The reduction is Cody and Waite's with
 // ln2 split in two (the leading part is the double nearest ln 2, the trailing
 // part the rest), each product taken by one FMA.  The scale 2^m goes into the
 // exponent field with an integer add.  |x| >= 708, infinities and NaN take
@@ -88,7 +91,9 @@ __device__ __forceinline__ double fexp(double x, const double* tab)
     double r = fma(-nd, l1, x);
     r = fma(-nd, l2, r);
     // q = (exp(r) - 1) / r by Horner's rule on the Taylor coefficients 1/k!
-#if PJG_EXP_BITS >= 6
+#if PJG_EXP_BITS >= 8
+    double q = 1.0 / 24;
+#elif PJG_EXP_BITS >= 6
     double q = fma(r, 1.0 / 120, 1.0 / 24);
 #elif PJG_EXP_BITS >= 4
     double q = fma(r, 1.0 / 40320, 1.0 / 5040);
