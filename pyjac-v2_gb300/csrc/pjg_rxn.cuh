@@ -311,8 +311,8 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
     const double mod = ldg(p + P_MOD);
     const bool hasns = flags & RX_HASNS;
     // temperature column (dRopi_dT :2589-3108, dci_*_dT :2117-2588)
-    double d0 = rf * dlnkf_dT;
-    if (rev) d0 = d0 + -1.0 * rr * (dlnkf_dT + -1.0 * dB);
+    // rf dlnkf - rr (dlnkf - dB) = Rnet dlnkf + rr dB
+    double d0 = rev ? fma(rr, dB, Rnet * dlnkf_dT) : rf * dlnkf_dT;
     d0 = d0 * ci_ * V;
     if (hasns) d0 += -gns * V * ci_ * PoRT * Tjinv;
     // extra-variable column (dRopi_dE :1458-1594, dci_*_dE :362-880)
@@ -440,10 +440,7 @@ __device__ __forceinline__ void e22_terms_v(const E22Head& h, const E22Vals& vv,
     const double b = ldg(p + P_B), Ta = ldg(p + P_TA);
     const double kf = arrhenius(RX_FORM(h.flags), ldg(p + P_A), b, Ta, h.bint, sv.Tc, sv.logT,
                                 sv.Tinv, sv.etab);
-    double Bsum = 0.0 - vv.b[0];
-    Bsum = Bsum - vv.b[1];
-    Bsum = Bsum + vv.b[2];
-    Bsum = Bsum + vv.b[3];
+    const double Bsum = (vv.b[2] + vv.b[3]) - (vv.b[0] + vv.b[1]);
     const double kr = kf * fexp(-min_pos(EXP_MAX, Bsum), sv.etab);
     const double c0 = vv.c[0], c1 = vv.c[1], c2 = vv.c[2], c3 = vv.c[3];
     // rounded products and difference (no contraction into an FMA): the rate
@@ -453,10 +450,7 @@ __device__ __forceinline__ void e22_terms_v(const E22Head& h, const E22Vals& vv,
     o.net = __dsub_rn(rf, rr);
     if (!DER) return;
     const double dlnkf_dT = (b + Ta * sv.Tjinv) * sv.Tjinv;
-    double dB = 0.0 - vv.db[0];
-    dB = dB - vv.db[1];
-    dB = dB + vv.db[2];
-    dB = dB + vv.db[3];
+    const double dB = (vv.db[2] + vv.db[3]) - (vv.db[0] + vv.db[1]);
     o.g[0] = kf * gsmall(c1);
     o.g[1] = kf * gsmall(c0);
     o.g[2] = -(kr * gsmall(c3));
@@ -467,9 +461,8 @@ __device__ __forceinline__ void e22_terms_v(const E22Head& h, const E22Vals& vv,
         if (h.s[j] == last) gns = o.g[j];
     o.gns = gns;
     const bool hasns = h.flags & RX_HASNS;
-    double d0 = rf * dlnkf_dT;
-    d0 = d0 + -1.0 * rr * (dlnkf_dT + -1.0 * dB);
-    d0 = d0 * sv.V;
+    // rf dlnkf - rr (dlnkf - dB) = net dlnkf + rr dB
+    double d0 = fma(rr, dB, o.net * dlnkf_dT) * sv.V;
     if (hasns) d0 += -gns * sv.V * sv.PoRT * sv.Tjinv;
     double d1 = sv.conp ? -rf + rr : 0.0;
     if (hasns) d1 += gns * (sv.conp ? sv.PoRT : sv.V * sv.rt_inv);
@@ -556,11 +549,21 @@ __device__ __forceinline__ void ma_terms(const RxnHead& h, int last, const State
     }
     double kr = 0.0, dB = 0.0;
     if (PT::rev) {
+        // the first term starts the sums (no addition to zero)
         double Bsum = 0.0;
+        bool first = true;
 #pragma unroll
         for (int e = 0; e < N; ++e) {
-            Bsum = addnu(Bsum, PT::nur(e) - PT::nuf(e), bk[sp[e]]);
-            if (DER) dB = addnu(dB, PT::nur(e) - PT::nuf(e), db[sp[e]]);
+            const int nu = PT::nur(e) - PT::nuf(e);
+            if (nu == 0) continue;
+            if (first) {
+                Bsum = nux(nu, bk[sp[e]]);
+                if (DER) dB = nux(nu, db[sp[e]]);
+                first = false;
+            } else {
+                Bsum = addnu(Bsum, nu, bk[sp[e]]);
+                if (DER) dB = addnu(dB, nu, db[sp[e]]);
+            }
         }
         kr = kf * ldg(p + P_PSUM) * fexp(-min_pos(EXP_MAX, Bsum), sv.etab);
     }
@@ -609,9 +612,8 @@ __device__ __forceinline__ void ma_terms(const RxnHead& h, int last, const State
     }
     o.gns = gns;
     const bool hasns = h.flags & RX_HASNS;
-    double d0 = rf * dlnkf_dT;
-    if (PT::rev) d0 = d0 + -1.0 * rr * (dlnkf_dT + -1.0 * dB);
-    d0 = d0 * sv.V;
+    // rf dlnkf - rr (dlnkf - dB) = net dlnkf + rr dB
+    double d0 = (PT::rev ? fma(rr, dB, o.net * dlnkf_dT) : rf * dlnkf_dT) * sv.V;
     if (hasns) d0 += -gns * sv.V * sv.PoRT * sv.Tjinv;
     double d1 = 0.0;
     if (sv.conp) d1 = -nux(PT::sumf() - 1, rf) + (PT::rev ? nux(PT::sumr() - 1, rr) : 0.0);

@@ -1,7 +1,7 @@
 """The packed reaction order of the device tables (host logic, no GPU).
 
 The evaluation kernels run reactions in groups, each compiled for its
-stoichiometry: the elementary class A + B <=> C + D, eight mass-action
+stoichiometry: the elementary class A + B <=> C + D, ten mass-action
 patterns without third body and three third-body / fall-off patterns, then
 the general code for the rest.  pjg_reaction_order returns the library's
 packing; here it is checked against a plain restatement of the rules on the
