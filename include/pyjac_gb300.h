@@ -128,7 +128,7 @@ int pjg_vjp(pjg_mech* mech, int64_t n, char order, int conp, const double* param
  * No counterpart in the reference.  Scratch is a fixed 16 MiB array inside
  * the library on each device, held until the process exits; larger problems
  * run as several launches on `stream`; mechanisms needing more than 16 MiB
- * per 128 states (about 1,800 species) are rejected with PJG_ERR_ARG.  The
+ * per 128 states (more than 1,638 species) are rejected with PJG_ERR_ARG.  The
  * first call on a device takes the array's address (call it before any
  * stream capture).  All calls share the array: calls that overlap on the GPU
  * race. */

@@ -67,6 +67,7 @@ struct SlotTables {
     int *row_off = nullptr, *col_off = nullptr;
     int2 *row_list = nullptr, *col_list = nullptr;
     int *sp_slots = nullptr, *cj_slots = nullptr;
+    int *dchunk_off = nullptr, *dchunk_list = nullptr;  // dense output only
     int s00 = 0, s01 = 0, s10 = 0, s11 = 0;
     size_t bytes = 0;
 };
@@ -86,6 +87,7 @@ extern "C" int pjg_internal_lu_solve_sparse(const void* p, int64_t n, char order
 struct pjg_mech {
     int ns = 0, nr = 0, nn = 0, need_logP = 0, nnz = 0, jac_approx = 0;
     int nr_e22 = 0;  // leading reactions of the class A + B <=> C + D
+    double kc_split_max = 138.0;  // EvalArgs::kc_split_max
     int ma_off[11] = {};                          // then the mass-action patterns (EvalArgs)
     int tp_off[4] = {0, 0, 0, 0};                 // then the third-body patterns (EvalArgs)
     int device = 0;
@@ -212,6 +214,33 @@ int build_slots(pjg_mech* m, bool F, bool sparse, SlotTables** out)
     }
     row_off[last] = (int)row_list.size();
     col_off[last] = (int)col_list.size();
+    // dense output: the structurally nonzero entries of the species block (the
+    // pattern's and every entry a reaction adds to) in chunks of
+    // PJG_DENSE_COLS columns, the assembly's row lists
+    std::vector<int> doff, dlist;
+    if (!sparse && last > 0) {
+        std::vector<char> nz((size_t)last * last, 0);
+        for (int k = 0; k < last; ++k)
+            for (int q = m->crs_ptr[2 + k]; q < m->crs_ptr[3 + k]; ++q) {
+                const int c = m->crs_ind[q] - 2;
+                if (c >= 0 && c < last) nz[(size_t)k * last + c] = 1;
+            }
+        for (int sl : list) {
+            if (sl < 0) continue;
+            const int r = F ? sl % NN : sl / NN, c = F ? sl / NN : sl % NN;
+            if (r >= 2 && c >= 2) nz[(size_t)(r - 2) * last + (c - 2)] = 1;
+        }
+        for (int j0 = 0; j0 < last; j0 += PJG_DENSE_COLS) {
+            doff.push_back((int)dlist.size());
+            for (int k = 0; k < last; ++k) {
+                int mask = 0;
+                for (int q = 0; q < PJG_DENSE_COLS && j0 + q < last; ++q)
+                    if (nz[(size_t)k * last + j0 + q]) mask |= 1 << q;
+                if (mask) dlist.push_back(k << 4 | mask);
+            }
+        }
+        doff.push_back((int)dlist.size());
+    }
     t.s00 = slot_of(m, F, sparse, 0, 0);
     t.s01 = slot_of(m, F, sparse, 0, 1);
     t.s10 = slot_of(m, F, sparse, 1, 0);
@@ -222,10 +251,12 @@ int build_slots(pjg_mech* m, bool F, bool sparse, SlotTables** out)
     if ((rc = upload(off, &t.rxn_slot_off)) || (rc = upload(list, &t.rxn_slots)) ||
         (rc = upload(row_off, &t.row_off)) || (rc = upload(row_list, &t.row_list)) ||
         (rc = upload(col_off, &t.col_off)) || (rc = upload(col_list, &t.col_list)) ||
-        (rc = upload(sp_slots, &t.sp_slots)) || (rc = upload(cj_slots, &t.cj_slots)))
+        (rc = upload(sp_slots, &t.sp_slots)) || (rc = upload(cj_slots, &t.cj_slots)) ||
+        (rc = upload(doff, &t.dchunk_off)) || (rc = upload(dlist, &t.dchunk_list)))
         return rc;
     t.bytes = (off.size() + list.size() + row_off.size() + col_off.size() + sp_slots.size() +
-               cj_slots.size()) * sizeof(int) + (row_list.size() + col_list.size()) * sizeof(int2);
+               cj_slots.size() + doff.size() + dlist.size()) * sizeof(int) +
+              (row_list.size() + col_list.size()) * sizeof(int2);
     auto res = m->slots.emplace(key, t);
     *out = &res.first->second;
     return 0;
@@ -310,6 +341,7 @@ void fill_common(const pjg_mech* m, EvalArgs& a)
     for (int q = 0; q <= pjg::kTpPatterns; ++q) a.tp_off[q] = m->tp_off[q];
     a.need_logP = m->need_logP;
     a.jac_approx = m->jac_approx;
+    a.kc_split_max = m->kc_split_max;
 }
 
 // Per-state bytes of working arrays one evaluation needs.  The Jacobian
@@ -408,6 +440,8 @@ int run_eval(pjg_mech* m, int kind, int64_t n, char order, int conp, int jac_for
             a.col_list = t->col_list;
             a.sp_slots = t->sp_slots;
             a.cj_slots = t->cj_slots;
+            a.dchunk_off = t->dchunk_off;
+            a.dchunk_list = t->dchunk_list;
             a.s00 = t->s00;
             a.s01 = t->s01;
             a.s10 = t->s10;
@@ -624,6 +658,20 @@ void order_reactions(pjg_mech* m)
     m->nr_e22 = pk.nr_e22;
     for (int q = 0; q <= pjg::kMaPatterns; ++q) m->ma_off[q] = pk.ma_off[q];
     for (int q = 0; q <= pjg::kTpPatterns; ++q) m->tp_off[q] = pk.tp_off[q];
+    // bound on a state's |b_k| under which 1 / Kc is formed from per-species
+    // factors: 690 / (largest sum |nu| of a reversible reaction), at most
+    // 690 / 5 (every coefficient pattern has sum |nu| <= 5)
+    int numax = 5;
+    for (const PjgRxn& R : m->h_rxn) {
+        if (!(R.flags & RX_REV)) continue;
+        int n = 0;
+        for (int e = 0; e < R.nspec; ++e) {
+            const int nu = ent_nur(R.ent[e]) - ent_nuf(R.ent[e]);
+            n += nu < 0 ? -nu : nu;
+        }
+        numax = std::max(numax, n);
+    }
+    m->kc_split_max = 690.0 / numax;
 }
 
 }  // namespace
@@ -909,6 +957,8 @@ int pjg_mech_destroy(pjg_mech* m)
         cudaFree(t.col_list);
         cudaFree(t.sp_slots);
         cudaFree(t.cj_slots);
+        cudaFree(t.dchunk_off);
+        cudaFree(t.dchunk_list);
     }
     delete m;
     return 0;

@@ -75,7 +75,10 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     auto arr = [&](int which) -> SV {
         return SV{a.scratch + (int64_t)which * ns * a.sc_ld + s, a.sc_ld};
     };
-    SV conc = arr(ARR_CONC), bk = arr(ARR_B), wdot = arr(ARR_WDOT);
+    // ep holds b_k until the state's split is known (then exp(b_k) if it
+    // holds); the per-reaction fallback reads b_k from it as bk
+    SV conc = arr(ARR_CONC), ep = arr(ARR_EP), em = arr(ARR_EM), wdot = arr(ARR_WDOT);
+    const SV& bk = ep;
     SV db{nullptr, 0}, nsrow{nullptr, 0}, hw{nullptr, 0}, cpa{nullptr, 0}, dcpa{nullptr, 0},
         ha{nullptr, 0};
     if (DER) {
@@ -124,8 +127,14 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     conc[last] = P / (RU * Tc) + -1.0 * gsmall(nsum) * Vinv;
     wdot[last] = 0.0;
 
-    // thermo: Gibbs functions for Kc (+ derivatives and cp, h for the Jacobian)
+    // thermo: Gibbs functions for Kc (+ derivatives and cp, h for the Jacobian),
+    // and their exponentials, the factors of 1 / Kc (StateVars::split)
     double h_ns = 0.0, cp_ns = 0.0, dcp_ns = 0.0;
+    bool split = true;
+    auto gibbs = [&](int k, double b) {
+        ep[k] = b;
+        split = split && abs_le(b, a.kc_split_max);
+    };
     if (DER) {
         const Thermo tl = thermo<true>(a.sp + (int64_t)last * PJG_SP_DOUBLES, Tc, logT, Tinv, conp);
         h_ns = tl.h;
@@ -134,7 +143,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         for (int k = 0; k < ns; ++k) {
             const double* rec = a.sp + (int64_t)k * PJG_SP_DOUBLES;
             const Thermo t = k == last ? tl : thermo<true>(rec, Tc, logT, Tinv, conp);
-            bk[k] = t.b;
+            gibbs(k, t.b);
             db[k] = t.db;
             ha[k] = t.h;
             if (k < last) {
@@ -145,8 +154,16 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         }
     } else {
         for (int k = 0; k < ns; ++k)
-            bk[k] = thermo<false>(a.sp + (int64_t)k * PJG_SP_DOUBLES, Tc, logT, Tinv, conp).b;
+            gibbs(k, thermo<false>(a.sp + (int64_t)k * PJG_SP_DOUBLES, Tc, logT, Tinv, conp).b);
     }
+    if (split) {
+        for (int k = 0; k < ns; ++k) {
+            const double b = ep[k];
+            ep[k] = fexp(b, etab);
+            em[k] = fexp(-b, etab);
+        }
+    }
+    sv.split = split;
 
     // J^T v: rows T and E of J are linear in the species rows, so v folds into
     // species weights vt_k = v_k + alpha * hw_k + beta * (1 - W_k/W_ns) known
@@ -177,14 +194,14 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     E22Vals vn;
     if (a.nr_e22 > 0) {
         load_e22(a.rxn, hn);
-        e22_fetch<DER>(hn, conc, bk, db, vn);
+        e22_fetch<DER>(hn, split, conc, ep, em, db, vn);
     }
     for (int i = 0; i < a.nr_e22; ++i) {
         const E22Head h = hn;
         const E22Vals vv = vn;
         if (i + 1 < a.nr_e22) {
             load_e22(a.rxn + i + 1, hn);
-            e22_fetch<DER>(hn, conc, bk, db, vn);
+            e22_fetch<DER>(hn, split, conc, ep, em, db, vn);
         }
         E22Terms o;
         e22_terms_v<DER>(h, vv, last, sv, o);
@@ -234,7 +251,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
             RxnHead h;
             load_head(a.rxn + i, h);
             MaTerms o;
-            ma_terms<PT, DER>(h, last, sv, conc, bk, db, o);
+            ma_terms<PT, DER>(h, last, sv, conc, bk, ep, em, db, o);
             int sp[N];
 #pragma unroll
             for (int e = 0; e < N; ++e) {
@@ -295,7 +312,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
             RxnHead h;
             load_head(a.rxn + i, h);
             RxnTerms o;
-            rxn_terms<DER, ST>(h, a.aux, a.thd_spec, a.thd_coef, last, sv, conc, bk, db, o);
+            rxn_terms<DER, ST>(h, a.aux, a.thd_spec, a.thd_coef, last, sv, conc, bk, ep, em, db, o);
             const int flags = h.flags, nsp = ST::nsp(h), thd_off = h.thd_off, thd_cnt = h.thd_cnt;
             const unsigned* ent = h.ent;
             const double* p = h.p;
@@ -484,45 +501,72 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     const double inv_vcp = 1.0 / (V * cp_tot);
     const double TRf = T * RU / fixed, eTj = extra * Tjinv;
     if (a.dense_rs) {
-        // Dense output: one pass over the species block, rows outer, in
-        // chunks of kCols columns whose row-T and row-E sums stay in
-        // registers.  A row's kCols entries are loaded together, have the
-        // row's bath-gas sum subtracted (stored back only then) and are
-        // summed into their columns' sums in increasing row order: the same
-        // operations in the same order as the two passes of the sparse
-        // branch, with each entry read once instead of twice.  Measured on
-        // 1M GRI states (dense F): 4 columns 92.1 ms, 6: 92.8, 8: 93.3, 10:
-        // 96.1, 16: 101.1 (register pressure), the two passes 96.3 ms; loads
-        // and stores interleaved entry by entry serialise on possible
-        // aliasing (100.4 ms).
-        constexpr int kCols = 4;
+        // Dense output: one pass over the species block, in chunks of kCols
+        // columns whose row-T and row-E sums stay in registers, visiting only
+        // the rows with a structurally nonzero entry in the chunk (dchunk_list;
+        // GRI: 1,774 of 2,704 entries).  A row's entries are loaded together,
+        // have the row's bath-gas sum subtracted (stored back only then) and
+        // are summed into their columns' sums in increasing row order: the same
+        // operations in the same order as the two passes of the sparse branch,
+        // with each entry read once instead of twice.  Entries outside the
+        // structure are zero, untouched.  Measured on 1M GRI states (dense F,
+        // every entry visited): 4 columns 92.1 ms, 6: 92.8, 8: 93.3, 10: 96.1,
+        // 16: 101.1 (register pressure), the two passes 96.3 ms; loads and
+        // stores interleaved entry by entry serialise on possible aliasing
+        // (100.4 ms).
+        constexpr int kCols = PJG_DENSE_COLS;
         const int rs = a.dense_rs, cs = a.dense_cs;
-        for (int j0 = 0; j0 < last; j0 += kCols) {
+        for (int c = 0, j0 = 0; j0 < last; ++c, j0 += kCols) {
             double sT[kCols], sE[kCols];
 #pragma unroll
             for (int q = 0; q < kCols; ++q) {
                 sT[q] = 0.0;
                 sE[q] = 0.0;
             }
-            for (int k = 0; k < last; ++k) {
+            const int t1 = __ldg(a.dchunk_off + c + 1);
+            for (int t = __ldg(a.dchunk_off + c); t < t1; ++t) {
+                const int e = __ldg(a.dchunk_list + t);  // the same for every thread
+                const int k = e >> 4, mask = e & 15;
                 double* rowp = acc + (int64_t)((2 + k) * rs) * ld;
-                double Jv[kCols];
-#pragma unroll
-                for (int q = 0; q < kCols; ++q)
-                    Jv[q] = j0 + q < last ? __ldcg(rowp + (int64_t)((2 + j0 + q) * cs) * ld) : 0.0;
                 const double v = rd(nsrow, k), hwk = hw[k];
                 const double omk = ldg(a.sp + (int64_t)k * PJG_SP_DOUBLES + SP_OMW);
-                if (nonzero(v)) {
+                double Jv[kCols];
+                if (mask == (1 << kCols) - 1) {
+#pragma unroll
+                    for (int q = 0; q < kCols; ++q)
+                        Jv[q] = __ldcg(rowp + (int64_t)((2 + j0 + q) * cs) * ld);
+                    if (nonzero(v)) {
+#pragma unroll
+                        for (int q = 0; q < kCols; ++q) {
+                            Jv[q] = Jv[q] - v;
+                            rowp[(int64_t)((2 + j0 + q) * cs) * ld] = Jv[q];
+                        }
+                    }
 #pragma unroll
                     for (int q = 0; q < kCols; ++q) {
-                        Jv[q] = Jv[q] - v;
-                        if (j0 + q < last) rowp[(int64_t)((2 + j0 + q) * cs) * ld] = Jv[q];
+                        sT[q] = fma(hwk, Jv[q], sT[q]);
+                        sE[q] = fma(omk, Jv[q], sE[q]);
                     }
-                }
+                } else {
 #pragma unroll
-                for (int q = 0; q < kCols; ++q) {
-                    sT[q] = fma(hwk, Jv[q], sT[q]);
-                    sE[q] = fma(omk, Jv[q], sE[q]);
+                    for (int q = 0; q < kCols; ++q)
+                        if (mask >> q & 1) Jv[q] = __ldcg(rowp + (int64_t)((2 + j0 + q) * cs) * ld);
+                    if (nonzero(v)) {
+#pragma unroll
+                        for (int q = 0; q < kCols; ++q) {
+                            if (mask >> q & 1) {
+                                Jv[q] = Jv[q] - v;
+                                rowp[(int64_t)((2 + j0 + q) * cs) * ld] = Jv[q];
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < kCols; ++q) {
+                        if (mask >> q & 1) {
+                            sT[q] = fma(hwk, Jv[q], sT[q]);
+                            sE[q] = fma(omk, Jv[q], sE[q]);
+                        }
+                    }
                 }
             }
 #pragma unroll

@@ -5,11 +5,16 @@
 #include "pjg_tables.cuh"
 
 #define PJG_BLOCK 128
+// columns of the species block whose row-T and row-E sums the dense assembly
+// keeps in registers at a time
+#define PJG_DENSE_COLS 4
 
 // per-state arrays (each ns doubles)
 enum {
     ARR_CONC = 0,  // concentrations c_k
-    ARR_B,         // Gibbs function b_k (Kc)
+    ARR_EP,        // exp(b_k), the reactant factor of 1 / Kc, where the state's
+                   // |b| allow (StateVars::split); else the Gibbs function b_k
+    ARR_EM,        // exp(-b_k), the product factor of 1 / Kc (split states)
     ARR_WDOT,      // net molar production rates
     ARR_N_RATES,
     ARR_DB = ARR_N_RATES,  // d b_k / dT
@@ -34,6 +39,9 @@ struct EvalArgs {
                      // ma_off[0] = nr_e22
     int tp_off[4];   // then [tp_off[q], tp_off[q + 1]) of third-body pattern q (TpP0..TpP2),
                      // tp_off[0] = ma_off[10]; the others from tp_off[3]
+    // 690 / (largest sum |nu| of a reversible reaction), at most 138: the bound
+    // on every |b_k| of a state for the per-species factors of 1 / Kc
+    double kc_split_max;
     int need_logP;
     int jac_approx;  // 'approximate' Jacobian type: no bath-gas terms in the species columns
     // states
@@ -64,6 +72,12 @@ struct EvalArgs {
     // dense output: slot of (row r, column c) = r * dense_rs + c * dense_cs
     // (0, 0 for a sparse output, whose slots come from the tables)
     int dense_rs, dense_cs;
+    // dense output: for species columns [PJG_DENSE_COLS c, PJG_DENSE_COLS (c + 1)),
+    // entries dchunk_list[dchunk_off[c] .. dchunk_off[c + 1]) = k << 4 | mask, the
+    // species rows k (increasing) with a structurally nonzero entry there, bit q
+    // of mask for column PJG_DENSE_COLS c + q
+    const int* dchunk_off;
+    const int* dchunk_list;
     // vector-Jacobian product
     const double* v;          // v[s * phi_ss + j * phi_sj]
     double* vjp;              // same layout

@@ -45,34 +45,47 @@ __device__ __forceinline__ double mulpow(double acc, double v, int p)
 
 // Table of 2^(j/2^B), j = 0 .. 2^B - 1, in shared memory (B = PJG_EXP_BITS):
 // every kernel that calls fexp fills one per block with fill_exp_table before
-// its first use.  B = 8 (256 entries, 2 KB) is the default: its polynomial
-// has one FMA fewer than B = 6's.  The random lookups meet bank conflicts,
-// which B = 4 (16 entries, one bank pair each) avoids and B = 0 (no table)
-// does without, both at the price of a longer polynomial.  Measured on GB300
-// (1,048,576 GRI-Mech 3.0 states, F order): B = 4 and B = 0 against B = 6, the
-// Jacobian kernel 2.6 % and 8.3 % slower, the species-rate kernel 13 % and
-// 30 % slower; B = 8 against B = 6, the Jacobian 73.5 against 74.3 ms and the
-// species rates 29.0 against 30.1 ms.  The FP64 instruction count, not the
-// shared-memory lookups, sets the time.
+// its first use, copied from the generated pjg_exp2_table (B = 8, 10, 11).
+// B = 10 (1,024 entries, 8 KB) is the default: its degree-3 minimax
+// polynomial has one FMA fewer than B = 8's degree-4 Taylor polynomial.  The
+// random lookups meet bank conflicts, which B = 4 (16 entries, one bank pair
+// each) avoids and B = 0 (no table) does without, both at the price of a
+// longer polynomial.  Measured on GB300 (1,048,576 GRI-Mech 3.0 states, F
+// order): B = 4 and B = 0 against B = 6, the Jacobian kernel 2.6 % and 8.3 %
+// slower, the species-rate kernel 13 % and 30 % slower; B = 8 against B = 6,
+// the Jacobian 73.5 against 74.3 ms and the species rates 29.0 against 30.1
+// ms; later B = 10 against B = 8, the Jacobian 70.4 against 70.9 ms and the
+// species rates 23.3 against 24.2 ms.  B = 11 (16 KB per block) equals B = 10
+// on GRI and slows the 500-species mechanism's Jacobian by 13 %.  The FP64
+// instruction count, not the shared-memory lookups, sets the time.
 #ifndef PJG_EXP_BITS
-#define PJG_EXP_BITS 8
+#define PJG_EXP_BITS 10
 #endif
 #define PJG_EXP_TAB (1 << PJG_EXP_BITS)
+}  // namespace pjg
+#include "pjg_exp_table.h"  // pjg_exp2_table for B = 8, 10, 11 (gen_exp_table.py)
+namespace pjg {
 
 __device__ __forceinline__ void fill_exp_table(double* tab)
 {
     for (int j = threadIdx.x; j < PJG_EXP_TAB; j += blockDim.x)
+#ifdef PJG_EXP_HAVE_TABLE
+        tab[j] = pjg_exp2_table[j];
+#else
         tab[j] = exp2((double)j * (1.0 / PJG_EXP_TAB));
+#endif
 }
 
 // exp(x) by the table-driven method of P. T. P. Tang ("Table-driven
 // implementation of the exponential function in IEEE floating-point
 // arithmetic", ACM TOMS 15(2), 1989): x = (2^B m + j) ln2 / 2^B + r with
-// |r| <= ln2 / 2^(B+1), so exp(x) = 2^m 2^(j/2^B) exp(r), and exp(r) - 1 is
-// its Taylor polynomial, of degree 4 for B = 8 (|r| <= 0.00136, truncation
-// below 4e-17 relative), 5 for B = 6 (|r| <= 0.0055, below 4e-17), 7 for
-// B = 4 (|r| <= 0.022, below 2e-18) and 13 for B = 0 (|r| <= 0.35, below
-// 5e-18).  The reduction is Cody and Waite's with
+// |r| <= ln2 / 2^(B+1), so exp(x) = 2^m 2^(j/2^B) exp(r).  exp(r) is a
+// polynomial: of degree 3 for B = 10 and 11 with minimax coefficients
+// (gen_exp_table.py; |r| <= 3.4e-4, largest relative error 9.4e-17 for
+// B = 10), else the Taylor polynomial, of degree 4 for B = 8 (|r| <= 0.00136,
+// truncation below 4e-17 relative), 5 for B = 6 (|r| <= 0.0055, below
+// 4e-17), 7 for B = 4 (|r| <= 0.022, below 2e-18) and 13 for B = 0
+// (|r| <= 0.35, below 5e-18).  The reduction is Cody and Waite's with
 // ln2 split in two (the leading part is the double nearest ln 2, the trailing
 // part the rest), each product taken by one FMA.  The scale 2^m goes into the
 // exponent field with an integer add.  |x| >= 708, infinities and NaN take
@@ -91,7 +104,11 @@ __device__ __forceinline__ double fexp(double x, const double* tab)
     double r = fma(-nd, l1, x);
     r = fma(-nd, l2, r);
     // q = (exp(r) - 1) / r by Horner's rule on the Taylor coefficients 1/k!
-#if PJG_EXP_BITS >= 8
+    // (B >= 10: on the minimax coefficients of gen_exp_table.py)
+#if PJG_EXP_BITS >= 10
+    double q = fma(r, PJG_EXP_C3, PJG_EXP_C2);
+    q = fma(q, r, 1.0);
+#elif PJG_EXP_BITS >= 8
     double q = 1.0 / 24;
 #elif PJG_EXP_BITS >= 6
     double q = fma(r, 1.0 / 120, 1.0 / 24);
@@ -112,9 +129,11 @@ __device__ __forceinline__ double fexp(double x, const double* tab)
     q = fma(q, r, 1.0 / 120);
     q = fma(q, r, 1.0 / 24);
 #endif
+#if PJG_EXP_BITS < 10
     q = fma(q, r, 1.0 / 6);
     q = fma(q, r, 0.5);
     q = fma(q, r, 1.0);
+#endif
 #if PJG_EXP_BITS > 0
     const double tj = tab[n & (PJG_EXP_TAB - 1)];
     const double y = fma(tj, r * q, tj);
@@ -132,6 +151,12 @@ __device__ __forceinline__ double fexp(double x, const double* tab)
 __device__ __forceinline__ double min_pos(double c, double x)
 {
     return __double_as_longlong(x) < __double_as_longlong(c) ? x : c;
+}
+
+// |x| <= c for a positive constant c on the integer pipe (false for NaN)
+__device__ __forceinline__ bool abs_le(double x, double c)
+{
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) <= __double_as_longlong(c);
 }
 
 // x != 0.0 on the integer pipe (either zero compares equal, NaN unequal)

@@ -13,12 +13,12 @@
 //
 // The scratch array is kScratchDoubles doubles (16 MiB) on every device that
 // loads the library, held until the process exits.  It holds the kernel's
-// per-state working arrays (9 * Ns doubles per state, 3,816 bytes for
-// GRI-Mech 3.0), so one launch covers up to floor(16 MiB / (72 Ns bytes))
-// states rounded down to a multiple of 128 (4,352 for GRI-Mech 3.0); larger
+// per-state working arrays (10 * Ns doubles per state, 4,240 bytes for
+// GRI-Mech 3.0), so one launch covers up to floor(16 MiB / (80 Ns bytes))
+// states rounded down to a multiple of 128 (3,840 for GRI-Mech 3.0); larger
 // problems run as several launches in order on the caller's stream.  A
-// mechanism whose 128-state block does not fit (more than about 1,800
-// species) is rejected with PJG_ERR_ARG.
+// mechanism whose 128-state block does not fit (more than 1,638 species) is
+// rejected with PJG_ERR_ARG.
 //
 // Set-up: the first call on each device, with that device current, takes the
 // array's device address with cudaGetSymbolAddress (a host-side name of a

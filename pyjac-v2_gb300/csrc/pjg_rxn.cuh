@@ -67,6 +67,12 @@ struct StateVars {
     double rt_inv;  // 1 / (R T)
     double logP;    // ln P (PLOG / Chebyshev mechanisms only)
     bool conp;
+    // every |b_k| <= EvalArgs::kc_split_max = 690 / (the mechanism's largest
+    // sum |nu| of a reversible reaction): 1 / Kc is the product of the
+    // participants' exp(+-b_k) (no partial product past e^690, so the
+    // reference's clamp of sum nu b at 690.78 never acts); else
+    // exp(-sum nu b) per reaction from b_k
+    bool split;
     const double* etab;  // fexp table (shared memory)
 };
 
@@ -132,6 +138,29 @@ struct PatStoich {
     __device__ static constexpr int nur(const RxnHead&, int e) { return PT::nur(e); }
 };
 
+// exp(-sum nu b) as the product of the participants' per-species factors
+// exp(b_k)^-nu (nu < 0) and exp(-b_k)^nu (nu > 0), where StateVars::split
+// holds (no partial product then passes e^690).
+template <class ST, class ARR>
+__device__ __forceinline__ double inv_kc_split(const RxnHead& h, const ARR& ep, const ARR& em)
+{
+    double r = 1.0;
+    bool first = true;
+#pragma unroll
+    for (int e = 0; e < PJG_MAXSP; ++e) {
+        if (e >= ST::nsp(h)) break;
+        const int nu = ST::nur(h, e) - ST::nuf(h, e);
+        if (nu == 0) continue;
+        const int k = ent_spec(h.ent[e]);
+        const double f = nu < 0 ? ep[k] : em[k];
+        const int na = nu < 0 ? -nu : nu;
+        const double fn = na == 1 ? f : (na == 2 ? __dmul_rn(f, f) : powi(f, na));
+        r = first ? fn : __dmul_rn(r, fn);
+        first = false;
+    }
+    return r;
+}
+
 struct FallState {
     double Pr, Fi, A, B, Fc, lnFc, X, lnQ, kratio;
     double e1, e2, e3;  // Troe exponentials at the clamped temperature
@@ -141,7 +170,7 @@ template <bool DER, class ST = RunStoich, class ARR>
 __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                                           const int* thd_spec, const double* thd_coef, int last,
                                           const StateVars& sv, const ARR& conc, const ARR& bk,
-                                          const ARR& db, RxnTerms& o)
+                                          const ARR& ep, const ARR& em, const ARR& db, RxnTerms& o)
 {
     const int flags = h.flags, nsp = ST::nsp(h);
     const double* p = h.p;
@@ -166,17 +195,28 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
     // reverse rate: kr = kf / Kc, Kc = (P_atm/R)^nu_sum exp(sum nu b)
     double kr = 0.0, dB = 0.0;
     if (rev) {
-        double Bsum = 0.0;
+        if (DER) {
 #pragma unroll
-        for (int e = 0; e < PJG_MAXSP; ++e) {
-            if (e >= nsp) break;
-            const int nu = ST::nur(h, e) - ST::nuf(h, e);
-            if (nu != 0) {
-                Bsum = addnu(Bsum, nu, bk[ent_spec(h.ent[e])]);
-                if (DER) dB = addnu(dB, nu, db[ent_spec(h.ent[e])]);
+            for (int e = 0; e < PJG_MAXSP; ++e) {
+                if (e >= nsp) break;
+                const int nu = ST::nur(h, e) - ST::nuf(h, e);
+                if (nu != 0) dB = addnu(dB, nu, db[ent_spec(h.ent[e])]);
             }
         }
-        kr = kf * ldg(p + P_PSUM) * fexp(-min_pos(EXP_MAX, Bsum), et);
+        double ikc;
+        if (sv.split) {
+            ikc = inv_kc_split<ST>(h, ep, em);
+        } else {
+            double Bsum = 0.0;
+#pragma unroll
+            for (int e = 0; e < PJG_MAXSP; ++e) {
+                if (e >= nsp) break;
+                const int nu = ST::nur(h, e) - ST::nuf(h, e);
+                if (nu != 0) Bsum = addnu(Bsum, nu, bk[ent_spec(h.ent[e])]);
+            }
+            ikc = fexp(-min_pos(EXP_MAX, Bsum), et);
+        }
+        kr = kf * ldg(p + P_PSUM) * ikc;
     }
     // rates of progress (mass action on raw concentrations)
     double rf = kf, rr = kr;
@@ -415,19 +455,21 @@ struct E22Terms {
     double d0, d1;
 };
 
-// the per-state values one elementary reaction reads (loaded ahead of use)
+// the per-state values one elementary reaction reads (loaded ahead of use):
+// concentrations, the 1 / Kc factors exp(b) of the reactants and exp(-b) of
+// the products (in a split state; else the four b), d b / dT
 struct E22Vals {
-    double c[4], b[4], db[4];
+    double c[4], x[4], db[4];
 };
 
 template <bool DER, class ARR>
-__device__ __forceinline__ void e22_fetch(const E22Head& h, const ARR& conc, const ARR& bk,
-                                          const ARR& db, E22Vals& v)
+__device__ __forceinline__ void e22_fetch(const E22Head& h, bool split, const ARR& conc,
+                                          const ARR& ep, const ARR& em, const ARR& db, E22Vals& v)
 {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         v.c[q] = conc[h.s[q]];
-        v.b[q] = bk[h.s[q]];
+        v.x[q] = (q < 2 || !split) ? ep[h.s[q]] : em[h.s[q]];  // ep holds b if !split
         if (DER) v.db[q] = db[h.s[q]];
     }
 }
@@ -440,8 +482,14 @@ __device__ __forceinline__ void e22_terms_v(const E22Head& h, const E22Vals& vv,
     const double b = ldg(p + P_B), Ta = ldg(p + P_TA);
     const double kf = arrhenius(RX_FORM(h.flags), ldg(p + P_A), b, Ta, h.bint, sv.Tc, sv.logT,
                                 sv.Tinv, sv.etab);
-    const double Bsum = (vv.b[2] + vv.b[3]) - (vv.b[0] + vv.b[1]);
-    const double kr = kf * fexp(-min_pos(EXP_MAX, Bsum), sv.etab);
+    double ikc;  // 1 / Kc = exp(-sum nu b)
+    if (sv.split) {
+        ikc = __dmul_rn(__dmul_rn(vv.x[0], vv.x[1]), __dmul_rn(vv.x[2], vv.x[3]));
+    } else {
+        const double Bsum = (vv.x[2] + vv.x[3]) - (vv.x[0] + vv.x[1]);
+        ikc = fexp(-min_pos(EXP_MAX, Bsum), sv.etab);
+    }
+    const double kr = kf * ikc;
     const double c0 = vv.c[0], c1 = vv.c[1], c2 = vv.c[2], c3 = vv.c[3];
     // rounded products and difference (no contraction into an FMA): the rate
     // of progress must be the same in every kernel kind, whatever else uses
@@ -533,7 +581,8 @@ struct MaTerms {
 
 template <class PT, bool DER, class ARR>
 __device__ __forceinline__ void ma_terms(const RxnHead& h, int last, const StateVars& sv,
-                                         const ARR& conc, const ARR& bk, const ARR& db, MaTerms& o)
+                                         const ARR& conc, const ARR& bk, const ARR& ep,
+                                         const ARR& em, const ARR& db, MaTerms& o)
 {
     constexpr int N = PT::n;
     const double* p = h.p;
@@ -550,22 +599,30 @@ __device__ __forceinline__ void ma_terms(const RxnHead& h, int last, const State
     double kr = 0.0, dB = 0.0;
     if (PT::rev) {
         // the first term starts the sums (no addition to zero)
-        double Bsum = 0.0;
         bool first = true;
 #pragma unroll
         for (int e = 0; e < N; ++e) {
             const int nu = PT::nur(e) - PT::nuf(e);
-            if (nu == 0) continue;
-            if (first) {
-                Bsum = nux(nu, bk[sp[e]]);
-                if (DER) dB = nux(nu, db[sp[e]]);
-                first = false;
-            } else {
-                Bsum = addnu(Bsum, nu, bk[sp[e]]);
-                if (DER) dB = addnu(dB, nu, db[sp[e]]);
-            }
+            if (nu == 0 || !DER) continue;
+            dB = first ? nux(nu, db[sp[e]]) : addnu(dB, nu, db[sp[e]]);
+            first = false;
         }
-        kr = kf * ldg(p + P_PSUM) * fexp(-min_pos(EXP_MAX, Bsum), sv.etab);
+        double ikc;
+        if (sv.split) {
+            ikc = inv_kc_split<PatStoich<PT>>(h, ep, em);
+        } else {
+            double Bsum = 0.0;
+            first = true;
+#pragma unroll
+            for (int e = 0; e < N; ++e) {
+                const int nu = PT::nur(e) - PT::nuf(e);
+                if (nu == 0) continue;
+                Bsum = first ? nux(nu, bk[sp[e]]) : addnu(Bsum, nu, bk[sp[e]]);
+                first = false;
+            }
+            ikc = fexp(-min_pos(EXP_MAX, Bsum), sv.etab);
+        }
+        kr = kf * ldg(p + P_PSUM) * ikc;
     }
     // rounded products and difference: the rate of progress is the same in
     // every kernel kind (see e22_terms)

@@ -83,6 +83,51 @@ def test_temperatures_at_and_beyond_the_limits(cuda_device, name, order):
     _check(pkg("api").Evaluator(mech), mech, P, phi, order, True, cuda_device)
 
 
+def _gibbs_b(mech, T):
+    """b_k = S_k/R - H_k/(R T) - ln T of every species at each T (NASA-7), the
+    exponent of the equilibrium constants' per-species factors"""
+    out = np.empty((T.size, mech.n_species))
+    lnT = np.log(T)
+    for k, sp in enumerate(mech.species):
+        lo, hi = np.asarray(sp.lo, float), np.asarray(sp.hi, float)
+        a = np.where((T < sp.Trange[1])[:, None], lo[None, :], hi[None, :])
+        h = (a[:, 0] + T * (a[:, 1] / 2 + T * (a[:, 2] / 3 + T * (a[:, 3] / 4 + T * a[:, 4] / 5)))
+             + a[:, 5] / T)
+        s = a[:, 0] * lnT + T * (a[:, 1] + T * (a[:, 2] / 2 + T * (a[:, 3] / 3 + T * a[:, 4] / 4))) + a[:, 6]
+        out[:, k] = s - h - lnT
+    return out
+
+
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_equilibrium_constants_on_both_sides_of_the_split(cuda_device, order):
+    """1 / Kc is the product of per-species factors exp(+-b_k) in states whose
+    |b_k| are all at most 138, and exp(-sum nu b) per reaction in the others
+    (GRI below about 500 K): states of both kinds interleaved within every
+    warp, rates, Jacobian and J^T v against the oracle."""
+    mech = load_mech("gri30")
+    n = 256
+    rng = np.random.default_rng(41)
+    temps = np.where(np.arange(n) % 3 == 0, rng.uniform(250.0, 700.0, n), rng.uniform(700.0, 3000.0, n))
+    big = np.abs(_gibbs_b(mech, temps)).max(axis=1) > 138.0
+    assert 0.1 < big.mean() < 0.5
+    P, phi = pkg("states").draw_states(mech.n_species, n, seed=41, x_floor=1e-12)
+    phi = phi.copy()
+    phi[:, 2:] *= (phi[:, 0] / temps)[:, None]
+    phi[:, 0] = temps
+    ev = pkg("api").Evaluator(mech)
+    _check(ev, mech, P, phi, order, True, cuda_device)
+    v = rng.standard_normal(phi.shape)
+    J = oracle_mod().Oracle(mech).jacobian(P, phi)
+    ref = np.einsum("nrc,nr->nc", J, v)
+    scale = np.einsum("nrc,nr->nc", np.abs(J), np.abs(v))
+    x, vv = (phi, v) if order == "C" else (phi.T, v.T)
+    out = ev.vjp(_dev(P, cuda_device), _dev(x, cuda_device), _dev(vv, cuda_device),
+                 order=order).cpu().numpy()
+    out = out if order == "C" else out.T
+    assert np.isfinite(out).all()
+    assert (np.abs(out - ref) / np.where(scale > 0, scale, 1.0)).max() < 1e-9
+
+
 @pytest.mark.parametrize("order", ["C", "F"])
 def test_exact_zero_moles(cuda_device, order):
     """Species with exactly zero moles exercise the 1e-300 floors."""

@@ -70,7 +70,7 @@ def test_noalloc_vjp_matches_pjg_vjp_on_consecutive_calls(cuda_device, order):
     lib = L.load()
     mech = load_mech("gri30")
     dm = pkg("api").DeviceMechanism(mech)
-    n = 10000  # more than one 4,352-state chunk of the 16 MiB scratch for GRI-Mech 3.0
+    n = 10000  # more than one 3,840-state chunk of the 16 MiB scratch for GRI-Mech 3.0
     tP, tphi = _inputs(mech, n, order, cuda_device, 41)
     rng = np.random.default_rng(3)
     for call in range(2):
