@@ -99,6 +99,7 @@ struct pjg_mech {
     // host copies used to derive slot tables
     std::vector<PjgRxn> h_rxn;
     std::vector<int> h_thd_spec;
+    std::vector<double> h_thd_coef;
     std::vector<int> crs_ptr, crs_ind, ccs_ptr, ccs_ind;
     std::map<int, SlotTables> slots;  // key: (order == 'F') * 2 + sparse
     std::mutex lock;
@@ -608,7 +609,40 @@ struct Packing {
     int tp_off[pjg::kTpPatterns + 1] = {};
 };
 
-void pack_reactions(const std::vector<PjgRxn>& in, Packing& pk)
+// Reactions with a third body whose [M] is the same function of the state
+// (default efficiency, then the same (species, efficiency) list) share one
+// key: the mechanism-order index of the first such reaction.  -1 without a
+// third body.  canon receives that first reaction's list offset.
+std::vector<int> third_body_keys(const std::vector<PjgRxn>& in, const int* thd_spec,
+                                 const double* thd_coef, std::vector<int>& canon)
+{
+    std::map<std::vector<long long>, int> seen;
+    std::vector<int> key(in.size(), -1);
+    canon.assign(in.size(), 0);
+    for (int i = 0; i < (int)in.size(); ++i) {
+        const PjgRxn& R = in[i];
+        canon[i] = R.thd_off;
+        if (RX_THD(R.flags) == THD_NONE) continue;
+        std::vector<long long> k;
+        double flag = R.p[P_FLAG];
+        long long fb;
+        memcpy(&fb, &flag, sizeof fb);
+        k.push_back(fb);
+        for (int l = 0; l < R.thd_cnt; ++l) {
+            long long cb;
+            memcpy(&cb, thd_coef + R.thd_off + l, sizeof cb);
+            k.push_back(thd_spec[R.thd_off + l]);
+            k.push_back(cb);
+        }
+        auto it = seen.emplace(k, i).first;
+        key[i] = it->second;
+        canon[i] = in[it->second].thd_off;
+    }
+    return key;
+}
+
+void pack_reactions(const std::vector<PjgRxn>& in, const int* thd_spec, const double* thd_coef,
+                    Packing& pk)
 {
     const int nma = pjg::kMaPatterns, ntp = pjg::kTpPatterns;
     std::vector<std::vector<int>> groups(1 + nma + ntp + 1);  // indices into `in`
@@ -623,6 +657,28 @@ void pack_reactions(const std::vector<PjgRxn>& in, Packing& pk)
         }
         groups[g].push_back(i);
     }
+    // third-body groups and the general group: the later reactions sharing
+    // [M] with a reaction are moved up to follow it (every other reaction
+    // keeps its place in mechanism order), so that the kernels reuse [M] and
+    // ln [M]; identical lists share one stored copy
+    std::vector<int> canon;
+    const std::vector<int> key = third_body_keys(in, thd_spec, thd_coef, canon);
+    for (int g = 1 + nma; g < (int)groups.size(); ++g) {
+        std::vector<int> ordered;
+        std::vector<char> placed(groups[g].size(), 0);
+        for (size_t x = 0; x < groups[g].size(); ++x) {
+            if (placed[x]) continue;
+            const int i = groups[g][x];
+            ordered.push_back(i);
+            if (key[i] < 0) continue;
+            for (size_t y = x + 1; y < groups[g].size(); ++y)
+                if (!placed[y] && key[groups[g][y]] == key[i]) {
+                    ordered.push_back(groups[g][y]);
+                    placed[y] = 1;
+                }
+        }
+        groups[g].swap(ordered);
+    }
     pk.rx.clear();
     pk.orig.clear();
     pk.cls.clear();
@@ -632,6 +688,7 @@ void pack_reactions(const std::vector<PjgRxn>& in, Packing& pk)
         for (int i : groups[g]) {
             const PjgRxn& R = in[i];
             PjgRxn c = R;
+            c.thd_off = canon[i];
             if (g == 0) {
                 int q = 0;
                 for (int side = 0; side < 2; ++side)
@@ -639,6 +696,7 @@ void pack_reactions(const std::vector<PjgRxn>& in, Packing& pk)
                         if ((ent_nuf(R.ent[e]) == 1) == (side == 0)) c.ent[q++] = R.ent[e];
             } else if (g <= nma + ntp) {
                 c = canonical_entries(R);
+                c.thd_off = canon[i];
             }
             pk.rx.push_back(c);
             pk.orig.push_back(i);
@@ -648,12 +706,32 @@ void pack_reactions(const std::vector<PjgRxn>& in, Packing& pk)
         if (g == nma) pk.ma_off[nma] = (int)pk.rx.size();
         if (g == nma + ntp) pk.tp_off[ntp] = (int)pk.rx.size();
     }
+    // RX_SAMEM: [M] equals the previous reaction's in the same group;
+    // RX_SAMELNM: and an earlier reaction of that run formed ln [M] (a Troe or
+    // SRI fall-off with both rate constants in exponential form, which forms
+    // it whatever Pr)
+    const int nr = (int)pk.rx.size();
+    bool run_log = false;
+    for (int q = 0; q < nr; ++q) {
+        PjgRxn& c = pk.rx[q];
+        c.flags &= ~(RX_SAMEM | RX_SAMELNM);
+        const int g = pk.cls[q];
+        const bool same = q > 0 && key[pk.orig[q]] >= 0 && key[pk.orig[q]] == key[pk.orig[q - 1]] &&
+                          g == pk.cls[q - 1];
+        if (!same) run_log = false;
+        if (same) c.flags |= RX_SAMEM;
+        if (same && run_log) c.flags |= RX_SAMELNM;
+        const int blend = RX_BLEND(c.flags);
+        if (RX_THD(c.flags) != THD_NONE && (blend == BL_TROE || blend == BL_SRI) &&
+            RX_FORM(c.flags) == FORM_ARR && RX_FFORM(c.flags) == FORM_ARR)
+            run_log = true;
+    }
 }
 
 void order_reactions(pjg_mech* m)
 {
     Packing pk;
-    pack_reactions(m->h_rxn, pk);
+    pack_reactions(m->h_rxn, m->h_thd_spec.data(), m->h_thd_coef.data(), pk);
     m->h_rxn.swap(pk.rx);
     m->nr_e22 = pk.nr_e22;
     for (int q = 0; q <= pjg::kMaPatterns; ++q) m->ma_off[q] = pk.ma_off[q];
@@ -891,6 +969,7 @@ int pjg_mech_create(const pjg_tables* tb, pjg_mech** out)
     const PjgRxn* r = (const PjgRxn*)tb->rxn;
     m->h_rxn.assign(r, r + tb->nr);
     m->h_thd_spec.assign(tb->thd_spec, tb->thd_spec + std::max(tb->n_thd, 0));
+    m->h_thd_coef.assign(tb->thd_coef, tb->thd_coef + std::max(tb->n_thd, 0));
     for (const PjgRxn& R : m->h_rxn) {
         if (R.nspec < 1 || R.nspec > PJG_MAXSP || R.thd_off < 0 || R.thd_cnt < 0 ||
             R.thd_off + R.thd_cnt > tb->n_thd) {
@@ -972,8 +1051,12 @@ int pjg_reaction_order(const pjg_tables* tb, int32_t* orig, int32_t* cls)
     for (int i = 0; i < tb->nr; ++i)
         if (r[i].nspec < 1 || r[i].nspec > PJG_MAXSP)
             return fail(PJG_ERR_TABLES, "reaction record out of range");
+    for (int i = 0; i < tb->nr; ++i)
+        if (r[i].thd_off < 0 || r[i].thd_cnt < 0 || r[i].thd_off + r[i].thd_cnt > std::max(tb->n_thd, 0) ||
+            (r[i].thd_cnt > 0 && (!tb->thd_spec || !tb->thd_coef)))
+            return fail(PJG_ERR_TABLES, "reaction record out of range");
     Packing pk;
-    pack_reactions(std::vector<PjgRxn>(r, r + tb->nr), pk);
+    pack_reactions(std::vector<PjgRxn>(r, r + tb->nr), tb->thd_spec, tb->thd_coef, pk);
     for (int p = 0; p < tb->nr; ++p) {
         orig[p] = pk.orig[p];
         cls[p] = pk.cls[p];

@@ -59,6 +59,98 @@ struct SV {
 #define PJG_JAC_MINB 4  // resident 128-thread blocks per SM requested for the Jacobian kernel
 #endif
 
+// Rows T and E of a dense output and the bath-gas terms of its species
+// block (the assembly step of eval_kernel<1>), out of line so that its
+// registers do not shape the reaction loops' allocation.
+__device__ __noinline__ void dense_rows_te(double* acc, int64_t ld, int rs, int cs,
+                                           const int* dchunk_off, const int* dchunk_list,
+                                           const double* sp, SV nsrow, SV hw, SV cpa, int last,
+                                           double cp_ns, double Tdot, double inv_vcp, double TRf,
+                                           double eTj)
+{
+    constexpr int kCols = PJG_DENSE_COLS;
+    for (int c = 0, j0 = 0; j0 < last; ++c, j0 += kCols) {
+        double sT[kCols], sE[kCols];
+#pragma unroll
+        for (int q = 0; q < kCols; ++q) {
+            sT[q] = 0.0;
+            sE[q] = 0.0;
+        }
+        // software-pipelined: the next listed row's entries and weights
+        // are loaded before this row's are summed (and stored back)
+        auto fetch = [&](int e, double (&J)[kCols], double& v_, double& hw_, double& om_) {
+            const int k = e >> 4, mask = e & 15;
+            const double* rowp = acc + (int64_t)((2 + k) * rs) * ld;
+#pragma unroll
+            for (int q = 0; q < kCols; ++q)
+                J[q] = (mask >> q & 1) ? __ldcg(rowp + (int64_t)((2 + j0 + q) * cs) * ld) : 0.0;
+            v_ = __ldcg(&nsrow[k]);
+            hw_ = hw[k];
+            om_ = ldg(sp + (int64_t)k * PJG_SP_DOUBLES + SP_OMW);
+        };
+        int t = __ldg(dchunk_off + c);
+        const int t1 = __ldg(dchunk_off + c + 1);
+        int en = 0;
+        double Jn[kCols], vn = 0.0, hwn = 0.0, omn = 0.0;
+        if (t < t1) {
+            en = __ldg(dchunk_list + t);  // the same for every thread
+            fetch(en, Jn, vn, hwn, omn);
+        }
+        for (; t < t1; ++t) {
+            const int e = en, k = e >> 4, mask = e & 15;
+            double Jv[kCols];
+#pragma unroll
+            for (int q = 0; q < kCols; ++q) Jv[q] = Jn[q];
+            const double v = vn, hwk = hwn, omk = omn;
+            if (t + 1 < t1) {
+                en = __ldg(dchunk_list + t + 1);
+                fetch(en, Jn, vn, hwn, omn);
+            }
+            double* rowp = acc + (int64_t)((2 + k) * rs) * ld;
+            if (mask == (1 << kCols) - 1) {
+                if (nonzero(v)) {
+#pragma unroll
+                    for (int q = 0; q < kCols; ++q) {
+                        Jv[q] = Jv[q] - v;
+                        rowp[(int64_t)((2 + j0 + q) * cs) * ld] = Jv[q];
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < kCols; ++q) {
+                    sT[q] = fma(hwk, Jv[q], sT[q]);
+                    sE[q] = fma(omk, Jv[q], sE[q]);
+                }
+            } else {
+                if (nonzero(v)) {
+#pragma unroll
+                    for (int q = 0; q < kCols; ++q) {
+                        if (mask >> q & 1) {
+                            Jv[q] = Jv[q] - v;
+                            rowp[(int64_t)((2 + j0 + q) * cs) * ld] = Jv[q];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < kCols; ++q) {
+                    if (mask >> q & 1) {
+                        sT[q] = fma(hwk, Jv[q], sT[q]);
+                        sE[q] = fma(omk, Jv[q], sE[q]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kCols; ++q) {
+            const int j = j0 + q;
+            if (j < last) {
+                const double J0 = -1.0 * (sT[q] + Tdot * (cpa[j] + -1.0 * cp_ns)) * inv_vcp;
+                acc[(int64_t)(2 + j) * cs * ld] = J0;
+                acc[(int64_t)(rs + (2 + j) * cs) * ld] = TRf * sE[q] + eTj * J0;
+            }
+        }
+    }
+}
+
 template <int KIND>  // 0 species rates, 1 Jacobian, 2 J^T v
 __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND == 2 ? PJG_VJP_MINB : 4))
     eval_kernel(const EvalArgs a)
@@ -308,11 +400,12 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     // TpP0..TpP2 compiled per pattern, the rest reading their coefficients)
     auto general = [&](auto st_tag, int i0, int i1) {
         using ST = decltype(st_tag);
+        MCache mc;
         for (int i = i0; i < i1; ++i) {
             RxnHead h;
             load_head(a.rxn + i, h);
             RxnTerms o;
-            rxn_terms<DER, ST>(h, a.aux, a.thd_spec, a.thd_coef, last, sv, conc, bk, ep, em, db, o);
+            rxn_terms<DER, ST>(h, a.aux, a.thd_spec, a.thd_coef, last, sv, conc, bk, ep, em, db, mc, o);
             const int flags = h.flags, nsp = ST::nsp(h), thd_off = h.thd_off, thd_cnt = h.thd_cnt;
             const unsigned* ent = h.ent;
             const double* p = h.p;
@@ -514,71 +607,8 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
         // 16: 101.1 (register pressure), the two passes 96.3 ms; loads and
         // stores interleaved entry by entry serialise on possible aliasing
         // (100.4 ms).
-        constexpr int kCols = PJG_DENSE_COLS;
-        const int rs = a.dense_rs, cs = a.dense_cs;
-        for (int c = 0, j0 = 0; j0 < last; ++c, j0 += kCols) {
-            double sT[kCols], sE[kCols];
-#pragma unroll
-            for (int q = 0; q < kCols; ++q) {
-                sT[q] = 0.0;
-                sE[q] = 0.0;
-            }
-            const int t1 = __ldg(a.dchunk_off + c + 1);
-            for (int t = __ldg(a.dchunk_off + c); t < t1; ++t) {
-                const int e = __ldg(a.dchunk_list + t);  // the same for every thread
-                const int k = e >> 4, mask = e & 15;
-                double* rowp = acc + (int64_t)((2 + k) * rs) * ld;
-                const double v = rd(nsrow, k), hwk = hw[k];
-                const double omk = ldg(a.sp + (int64_t)k * PJG_SP_DOUBLES + SP_OMW);
-                double Jv[kCols];
-                if (mask == (1 << kCols) - 1) {
-#pragma unroll
-                    for (int q = 0; q < kCols; ++q)
-                        Jv[q] = __ldcg(rowp + (int64_t)((2 + j0 + q) * cs) * ld);
-                    if (nonzero(v)) {
-#pragma unroll
-                        for (int q = 0; q < kCols; ++q) {
-                            Jv[q] = Jv[q] - v;
-                            rowp[(int64_t)((2 + j0 + q) * cs) * ld] = Jv[q];
-                        }
-                    }
-#pragma unroll
-                    for (int q = 0; q < kCols; ++q) {
-                        sT[q] = fma(hwk, Jv[q], sT[q]);
-                        sE[q] = fma(omk, Jv[q], sE[q]);
-                    }
-                } else {
-#pragma unroll
-                    for (int q = 0; q < kCols; ++q)
-                        if (mask >> q & 1) Jv[q] = __ldcg(rowp + (int64_t)((2 + j0 + q) * cs) * ld);
-                    if (nonzero(v)) {
-#pragma unroll
-                        for (int q = 0; q < kCols; ++q) {
-                            if (mask >> q & 1) {
-                                Jv[q] = Jv[q] - v;
-                                rowp[(int64_t)((2 + j0 + q) * cs) * ld] = Jv[q];
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int q = 0; q < kCols; ++q) {
-                        if (mask >> q & 1) {
-                            sT[q] = fma(hwk, Jv[q], sT[q]);
-                            sE[q] = fma(omk, Jv[q], sE[q]);
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < kCols; ++q) {
-                const int j = j0 + q;
-                if (j < last) {
-                    const double J0 = -1.0 * (sT[q] + Tdot * (cpa[j] + -1.0 * cp_ns)) * inv_vcp;
-                    acc[(int64_t)(2 + j) * cs * ld] = J0;
-                    acc[(int64_t)(rs + (2 + j) * cs) * ld] = TRf * sE[q] + eTj * J0;
-                }
-            }
-        }
+        dense_rows_te(acc, ld, a.dense_rs, a.dense_cs, a.dchunk_off, a.dchunk_list, a.sp, nsrow, hw,
+                      cpa, last, cp_ns, Tdot, inv_vcp, TRf, eTj);
     } else {
         // sparse output: the bath-gas terms (per-row sums subtracted from every species
         // column of the pattern), then the column sums of rows T and E

@@ -186,6 +186,19 @@ __device__ __forceinline__ double arrhenius(int form, double A, double b, double
     return gexp(A + logT * b + -1.0 * Ta * Tinv, tab);
 }
 
+// the same, also giving ln k (the clamped exponent) for the exponential form
+// (has_ln false for the forms A and A T^b)
+__device__ __forceinline__ double arrhenius_ln(int form, double A, double b, double Ta, int bint,
+                                               double Tc, double logT, double Tinv,
+                                               const double* tab, double& lnk, bool& has_ln)
+{
+    has_ln = form > FORM_AT;
+    if (form == FORM_A) return A;
+    if (form == FORM_AT) return A * (bint < 0 ? powi(Tinv, -bint) : powi(Tc, bint));
+    lnk = min_pos(EXP_MAX, A + logT * b + -1.0 * Ta * Tinv);
+    return fexp(lnk, tab);
+}
+
 // PLOG: ln kf interpolated linearly in ln P between bracketing pressures,
 // clamped outside the table (rate_subs.py :2187-2224).  Returns ln kf, and
 // d ln kf / dT (explicit factor Tjinv = 1/T) and d ln kf / d ln P.

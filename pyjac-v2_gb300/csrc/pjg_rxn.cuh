@@ -161,8 +161,15 @@ __device__ __forceinline__ double inv_kc_split(const RxnHead& h, const ARR& ep, 
     return r;
 }
 
+// [M] of the last third-body reaction evaluated and ln [M] of the last
+// fall-off reaction that formed it: the packing makes reactions with the
+// same [M] adjacent and marks the repeats (RX_SAMEM, RX_SAMELNM)
+struct MCache {
+    double M = 0.0, logM = 0.0;
+};
+
 struct FallState {
-    double Pr, Fi, A, B, Fc, lnFc, X, lnQ, kratio;
+    double Pr, Fi, A, B, Fc, lnFc, X, lnQ, kratio, logPr;
     double e1, e2, e3;  // Troe exponentials at the clamped temperature
 };
 
@@ -170,7 +177,8 @@ template <bool DER, class ST = RunStoich, class ARR>
 __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                                           const int* thd_spec, const double* thd_coef, int last,
                                           const StateVars& sv, const ARR& conc, const ARR& bk,
-                                          const ARR& ep, const ARR& em, const ARR& db, RxnTerms& o)
+                                          const ARR& ep, const ARR& em, const ARR& db, MCache& mc,
+                                          RxnTerms& o)
 {
     const int flags = h.flags, nsp = ST::nsp(h);
     const double* p = h.p;
@@ -180,9 +188,11 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
     const double* et = sv.etab;
 
     // forward rate constant and its log-derivatives
-    double kf, dlnkf_dT = 0.0, dlnkf_dlnP = 0.0;
+    double kf, dlnkf_dT = 0.0, dlnkf_dlnP = 0.0, lnkf = 0.0;
+    bool has_lnkf = false;
     if (form <= FORM_ARR) {
-        kf = arrhenius(form, ldg(p + P_A), ldg(p + P_B), ldg(p + P_TA), h.bint, Tc, logT, Tinv, et);
+        kf = arrhenius_ln(form, ldg(p + P_A), ldg(p + P_B), ldg(p + P_TA), h.bint, Tc, logT, Tinv,
+                          et, lnkf, has_lnkf);
         if (DER) dlnkf_dT = (ldg(p + P_B) + ldg(p + P_TA) * Tjinv) * Tjinv;
     } else if (form == FORM_PLOG) {
         kf = gexp(plog_logk(aux + h.auxo, logT, Tinv, sv.logP, Tjinv, &dlnkf_dT, &dlnkf_dlnP), et);
@@ -234,20 +244,44 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
     double ci = 1.0, M = 0.0;
     FallState fs;
     fs.Pr = 0.0; fs.Fi = 1.0; fs.A = 0.0; fs.B = 0.0; fs.Fc = 1.0; fs.lnFc = 0.0; fs.X = 0.0;
-    fs.lnQ = 0.0; fs.kratio = 0.0; fs.e1 = 0.0; fs.e2 = 0.0; fs.e3 = 0.0;
+    fs.lnQ = 0.0; fs.kratio = 0.0; fs.e1 = 0.0; fs.e2 = 0.0; fs.e3 = 0.0; fs.logPr = 0.0;
     if (thd) {
-        M = sv.PoRT * ldg(p + P_FLAG);
-        for (int l = 0; l < h.thd_cnt; ++l)
-            M = fma(__ldg(thd_coef + h.thd_off + l), conc[__ldg(thd_spec + h.thd_off + l)], M);
+        if (flags & RX_SAMEM) {
+            M = mc.M;
+        } else {
+            M = sv.PoRT * ldg(p + P_FLAG);
+            for (int l = 0; l < h.thd_cnt; ++l)
+                M = fma(__ldg(thd_coef + h.thd_off + l), conc[__ldg(thd_spec + h.thd_off + l)], M);
+            mc.M = M;
+        }
         if (blend == BL_NONE) {
             ci = M;
         } else {
-            const double kfall = arrhenius(RX_FFORM(flags), ldg(p + P_FA), ldg(p + P_FB),
-                                           ldg(p + P_FTA), h.fbint, Tc, logT, Tinv, et);
+            double lnkfall = 0.0;
+            bool has_lnkfall = false;
+            const double kfall = arrhenius_ln(RX_FFORM(flags), ldg(p + P_FA), ldg(p + P_FB),
+                                              ldg(p + P_FTA), h.fbint, Tc, logT, Tinv, et,
+                                              lnkfall, has_lnkfall);
             fs.kratio = chem ? kf / kfall : kfall / kf;  // k0 / kinf
             fs.Pr = M * fs.kratio;
+            // log10 Pr: ln [M] (formed once per run of reactions sharing [M])
+            // + ln k0 - ln kinf where both rate constants are exponentials
+            // (the packing's rule for RX_SAMELNM) and Pr >= 1e-300; else the
+            // logarithm of the guarded Pr
+            if (blend == BL_TROE || blend == BL_SRI) {
+                double lnPr;
+                if (has_lnkf && has_lnkfall) {
+                    if (!(flags & RX_SAMELNM)) mc.logM = log(M);
+                    lnPr = __double_as_longlong(fs.Pr) >= __double_as_longlong(SMALL)
+                               ? mc.logM + (chem ? lnkf - lnkfall : lnkfall - lnkf)
+                               : log(SMALL);
+                } else {
+                    lnPr = log(gsmall(fs.Pr));
+                }
+                fs.logPr = lnPr * INV_LN10;
+            }
             if (blend == BL_TROE) {
-                const double logPr = log(gsmall(fs.Pr)) * INV_LN10;
+                const double logPr = fs.logPr;
                 const double ta = ldg(p + P_F0);
                 fs.e1 = gexp(-1.0 * Tc * ldg(p + P_F1), et);
                 fs.e3 = gexp(-1.0 * Tc * ldg(p + P_F3), et);
@@ -264,7 +298,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
                 const double B2 = fs.B * fs.B;
                 fs.Fi = fexp(B2 / (fs.A * fs.A + B2) * fs.lnFc, et);
             } else if (blend == BL_SRI) {
-                const double logPr = log(gsmall(fs.Pr)) * INV_LN10;
+                const double logPr = fs.logPr;
                 fs.X = 1.0 / (logPr * logPr + 1.0);
                 fs.e1 = gexp(-ldg(p + P_F1) * Tinv, et);
                 fs.e3 = gexp(-Tc / ldg(p + P_F2), et);
@@ -335,8 +369,7 @@ __device__ __forceinline__ void rxn_terms(const RxnHead& h, const double* aux,
             dlnFi_dPr = -2.0 * fs.A * fs.B * fs.lnFc * (0.14 * fs.A + fs.B) /
                         (gsmall(fs.Pr) * absq * absq * LN10);
         } else if (blend == BL_SRI) {
-            const double logPr = log(gsmall(fs.Pr)) * INV_LN10;
-            dlnFi_dPr = -2.0 * fs.X * fs.X * logPr / (gsmall(fs.Pr) * LN10) * fs.lnQ;
+            dlnFi_dPr = -2.0 * fs.X * fs.X * fs.logPr / (gsmall(fs.Pr) * LN10) * fs.lnQ;
         }
     }
     // d ci / dx given d Pr / dx = Pr theta + theta_n and the direct part of d ln Fi / dx

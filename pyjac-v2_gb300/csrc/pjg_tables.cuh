@@ -50,6 +50,9 @@
 #define RX_SRID (1 << 14)     // SRI d != 1
 #define RX_SRIE (1 << 15)     // SRI e != 0
 #define RX_SRIEINT (1 << 16)  // SRI e is integral
+// set by the library's packing (pjg_capi.cu), clear in the tables it is given:
+#define RX_SAMEM (1 << 20)    // [M] equals the previous packed reaction's (same group)
+#define RX_SAMELNM (1 << 21)  // and ln [M] was formed by an earlier reaction of that run
 
 #define RX_FORM(f) ((f) & RX_FORM_MASK)
 #define RX_THD(f) (((f) >> RX_THD_SHIFT) & 3)

@@ -6,8 +6,13 @@ patterns without third body and three third-body / fall-off patterns, then
 the general code for the rest.  pjg_reaction_order returns the library's
 packing; here it is checked against a plain restatement of the rules on the
 packed records of the mechanism: every reaction appears once, each group
-holds exactly the reactions the rules assign to it, in mechanism order, and
-the groups come in the order the kernels run them.
+holds exactly the reactions the rules assign to it, and the groups come in the
+order the kernels run them.  Within the elementary and mass-action groups the
+order is the mechanism's; within the third-body groups and the general group,
+the later reactions whose [M] is the same function of the state as an
+earlier one's (same default efficiency and (species, efficiency) list) are
+moved up to follow it, every other reaction keeping its mechanism order, so
+that the kernels form [M] and ln [M] once per list.
 """
 import numpy as np
 import pytest
@@ -41,6 +46,21 @@ def _key(rec):
             sorted(x for x in ents if x[0] == 0))
 
 
+def third_body_keys(tables):
+    """Per reaction: the mechanism index of the first reaction with the same
+    default efficiency and efficiency list, -1 without a third body."""
+    seen, keys = {}, []
+    for i, r in enumerate(tables.rxn):
+        if (int(r["flags"]) >> 4) & 3 == 0:
+            keys.append(-1)
+            continue
+        o, n = int(r["thd_off"]), int(r["thd_cnt"])
+        k = (float(r["p"][12]),) + tuple((int(tables.thd_spec[o + l]), float(tables.thd_coef[o + l]))
+                                         for l in range(n))
+        keys.append(seen.setdefault(k, i))
+    return np.array(keys)
+
+
 def expected_class(rec):
     flags = int(rec["flags"])
     form, rev, thd = flags & 7, bool(flags & 8), (flags >> 4) & 3
@@ -65,16 +85,29 @@ def expected_class(rec):
 def test_packing_matches_the_rules(name):
     mech = load_mech(name)
     orig, cls = pkg("api").reaction_order(mech)
-    rx = pkg("pack").PackedTables(mech).rxn
+    tables = pkg("pack").PackedTables(mech)
+    rx = tables.rxn
     assert sorted(orig.tolist()) == list(range(len(rx)))
     want = np.array([expected_class(rx[i]) for i in orig])
     assert np.array_equal(cls, want)
-    # groups in kernel order (elementary, patterns, general last), each in
-    # mechanism order
+    # groups in kernel order (elementary, patterns, general last)
     rank = np.where(cls < 0, 99, cls)
     assert np.all(np.diff(rank) >= 0)
+    key = third_body_keys(tables)
     for g in np.unique(rank):
-        assert np.all(np.diff(orig[rank == g]) > 0)
+        members = orig[rank == g]
+        if g <= 10:
+            assert np.all(np.diff(members) > 0)   # mechanism order
+        else:
+            want, done = [], set()
+            for i in sorted(members.tolist()):
+                if i in done:
+                    continue
+                same = [j for j in sorted(members.tolist()) if key[i] >= 0 and key[j] == key[i]]
+                for j in same or [i]:
+                    want.append(j)
+                    done.add(j)
+            assert members.tolist() == want
 
 
 def test_gri30_group_sizes():
