@@ -59,6 +59,14 @@ struct SV {
 #define PJG_JAC_MINB 4  // resident 128-thread blocks per SM requested for the Jacobian kernel
 #endif
 
+// Species-rate kernel: 6 blocks per SM fit its 80 registers without spills.
+// Measured on 1M GRI states (F): 4 blocks 22.35 ms, 5: 22.34, 6: 21.86, 8:
+// 21.75 (64 registers, with spills); the Jacobian at 5 blocks 68.7 against
+// 68.2 ms at 4, J^T v at 4 blocks 13.8 against 13.6 ms at 3.
+#ifndef PJG_RATES_MINB
+#define PJG_RATES_MINB 6  // resident 128-thread blocks per SM requested for the species-rate kernel
+#endif
+
 // Rows T and E of a dense output and the bath-gas terms of its species
 // block (the assembly step of eval_kernel<1>), out of line so that its
 // registers do not shape the reaction loops' allocation.
@@ -152,7 +160,7 @@ __device__ __noinline__ void dense_rows_te(double* acc, int64_t ld, int rs, int 
 }
 
 template <int KIND>  // 0 species rates, 1 Jacobian, 2 J^T v
-__global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND == 2 ? PJG_VJP_MINB : 4))
+__global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND == 2 ? PJG_VJP_MINB : PJG_RATES_MINB))
     eval_kernel(const EvalArgs a)
 {
     __shared__ double etab[PJG_EXP_TAB];
