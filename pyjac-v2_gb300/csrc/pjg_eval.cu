@@ -67,16 +67,32 @@ struct SV {
 #define PJG_RATES_MINB 6  // resident 128-thread blocks per SM requested for the species-rate kernel
 #endif
 
-// Rows T and E of a dense output and the bath-gas terms of its species
-// block (the assembly step of eval_kernel<1>), out of line so that its
-// registers do not shape the reaction loops' allocation.
-__device__ __noinline__ void dense_rows_te(double* acc, int64_t ld, int rs, int cs,
-                                           const int* dchunk_off, const int* dchunk_list,
-                                           const double* sp, SV nsrow, SV hw, SV cpa, int last,
-                                           double cp_ns, double Tdot, double inv_vcp, double TRf,
-                                           double eTj)
+// Rows T and E of the output and the bath-gas terms of its species block
+// (the assembly step of eval_kernel<1>), out of line so that its registers do
+// not shape the reaction loops' allocation.  One pass over the species block
+// in chunks of kCols columns whose row-T and row-E sums stay in registers,
+// visiting only the rows with a structurally nonzero entry in the chunk
+// (dchunk_list; GRI: 1,774 of 2,704 entries).  A row's entries are loaded
+// together, have the row's bath-gas sum subtracted (stored back only then)
+// and are summed into their columns' sums in increasing row order.  Slots:
+// (2 + k) rs + (2 + j) cs for a dense output, dchunk_slots (one quadruple per
+// listed row) and cj_slots for a sparse one.  Software-pipelined: the next
+// listed row's entries and weights are loaded before this row's are summed.
+// Measured on 1M GRI states (dense F): chunks of 4 columns 92.1 ms, 6: 92.8,
+// 8: 93.3, 10: 96.1, 16: 101.1 (register pressure), against 96.3 ms for two
+// passes (subtract, then sum); loads and stores interleaved entry by entry
+// serialised on possible aliasing (100.4 ms).  Later, with the row lists
+// 70.3 ms against every entry visited, pipelined 68.35 against 69.11 ms, out
+// of line 68.3 against 68.4 ms inlined.
+__device__ __noinline__ void rows_te(bool sparse, double* acc, int64_t ld, int rs, int cs,
+                                     const int* dchunk_off, const int* dchunk_list,
+                                     const int4* dchunk_slots, const int* cj_slots,
+                                     const double* sp, SV nsrow, SV hw, SV cpa, int last,
+                                     double cp_ns, double Tdot, double inv_vcp, double TRf,
+                                     double eTj)
 {
     constexpr int kCols = PJG_DENSE_COLS;
+    static_assert(kCols == 4, "one int4 of slots per listed row");
     for (int c = 0, j0 = 0; j0 < last; ++c, j0 += kCols) {
         double sT[kCols], sE[kCols];
 #pragma unroll
@@ -84,14 +100,22 @@ __device__ __noinline__ void dense_rows_te(double* acc, int64_t ld, int rs, int 
             sT[q] = 0.0;
             sE[q] = 0.0;
         }
-        // software-pipelined: the next listed row's entries and weights
-        // are loaded before this row's are summed (and stored back)
-        auto fetch = [&](int e, double (&J)[kCols], double& v_, double& hw_, double& om_) {
+        auto fetch = [&](int t, int e, double (&J)[kCols], int (&sl)[kCols], double& v_,
+                         double& hw_, double& om_) {
             const int k = e >> 4, mask = e & 15;
-            const double* rowp = acc + (int64_t)((2 + k) * rs) * ld;
+            if (sparse) {
+                const int4 q4 = __ldg(dchunk_slots + t);
+                sl[0] = q4.x;
+                sl[1] = q4.y;
+                sl[2] = q4.z;
+                sl[3] = q4.w;
+            } else {
+#pragma unroll
+                for (int q = 0; q < kCols; ++q) sl[q] = (2 + k) * rs + (2 + j0 + q) * cs;
+            }
 #pragma unroll
             for (int q = 0; q < kCols; ++q)
-                J[q] = (mask >> q & 1) ? __ldcg(rowp + (int64_t)((2 + j0 + q) * cs) * ld) : 0.0;
+                J[q] = (mask >> q & 1) ? __ldcg(acc + (int64_t)sl[q] * ld) : 0.0;
             v_ = __ldcg(&nsrow[k]);
             hw_ = hw[k];
             om_ = ldg(sp + (int64_t)k * PJG_SP_DOUBLES + SP_OMW);
@@ -99,28 +123,32 @@ __device__ __noinline__ void dense_rows_te(double* acc, int64_t ld, int rs, int 
         int t = __ldg(dchunk_off + c);
         const int t1 = __ldg(dchunk_off + c + 1);
         int en = 0;
+        int sln[kCols] = {0, 0, 0, 0};
         double Jn[kCols], vn = 0.0, hwn = 0.0, omn = 0.0;
         if (t < t1) {
             en = __ldg(dchunk_list + t);  // the same for every thread
-            fetch(en, Jn, vn, hwn, omn);
+            fetch(t, en, Jn, sln, vn, hwn, omn);
         }
         for (; t < t1; ++t) {
-            const int e = en, k = e >> 4, mask = e & 15;
+            const int mask = en & 15;
             double Jv[kCols];
+            int sl[kCols];
 #pragma unroll
-            for (int q = 0; q < kCols; ++q) Jv[q] = Jn[q];
+            for (int q = 0; q < kCols; ++q) {
+                Jv[q] = Jn[q];
+                sl[q] = sln[q];
+            }
             const double v = vn, hwk = hwn, omk = omn;
             if (t + 1 < t1) {
                 en = __ldg(dchunk_list + t + 1);
-                fetch(en, Jn, vn, hwn, omn);
+                fetch(t + 1, en, Jn, sln, vn, hwn, omn);
             }
-            double* rowp = acc + (int64_t)((2 + k) * rs) * ld;
             if (mask == (1 << kCols) - 1) {
                 if (nonzero(v)) {
 #pragma unroll
                     for (int q = 0; q < kCols; ++q) {
                         Jv[q] = Jv[q] - v;
-                        rowp[(int64_t)((2 + j0 + q) * cs) * ld] = Jv[q];
+                        acc[(int64_t)sl[q] * ld] = Jv[q];
                     }
                 }
 #pragma unroll
@@ -134,7 +162,7 @@ __device__ __noinline__ void dense_rows_te(double* acc, int64_t ld, int rs, int 
                     for (int q = 0; q < kCols; ++q) {
                         if (mask >> q & 1) {
                             Jv[q] = Jv[q] - v;
-                            rowp[(int64_t)((2 + j0 + q) * cs) * ld] = Jv[q];
+                            acc[(int64_t)sl[q] * ld] = Jv[q];
                         }
                     }
                 }
@@ -151,9 +179,11 @@ __device__ __noinline__ void dense_rows_te(double* acc, int64_t ld, int rs, int 
         for (int q = 0; q < kCols; ++q) {
             const int j = j0 + q;
             if (j < last) {
+                const int s0 = sparse ? __ldg(cj_slots + 2 * j) : (2 + j) * cs;
+                const int s1 = sparse ? __ldg(cj_slots + 2 * j + 1) : rs + (2 + j) * cs;
                 const double J0 = -1.0 * (sT[q] + Tdot * (cpa[j] + -1.0 * cp_ns)) * inv_vcp;
-                acc[(int64_t)(2 + j) * cs * ld] = J0;
-                acc[(int64_t)(rs + (2 + j) * cs) * ld] = TRf * sE[q] + eTj * J0;
+                acc[(int64_t)s0 * ld] = J0;
+                acc[(int64_t)s1 * ld] = TRf * sE[q] + eTj * J0;
             }
         }
     }
@@ -601,25 +631,15 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
     const double fixed = conp ? P : V, extra = conp ? V : P;
     const double inv_vcp = 1.0 / (V * cp_tot);
     const double TRf = T * RU / fixed, eTj = extra * Tjinv;
-    if (a.dense_rs) {
-        // Dense output: one pass over the species block, in chunks of kCols
-        // columns whose row-T and row-E sums stay in registers, visiting only
-        // the rows with a structurally nonzero entry in the chunk (dchunk_list;
-        // GRI: 1,774 of 2,704 entries).  A row's entries are loaded together,
-        // have the row's bath-gas sum subtracted (stored back only then) and
-        // are summed into their columns' sums in increasing row order: the same
-        // operations in the same order as the two passes of the sparse branch,
-        // with each entry read once instead of twice.  Entries outside the
-        // structure are zero, untouched.  Measured on 1M GRI states (dense F,
-        // every entry visited): 4 columns 92.1 ms, 6: 92.8, 8: 93.3, 10: 96.1,
-        // 16: 101.1 (register pressure), the two passes 96.3 ms; loads and
-        // stores interleaved entry by entry serialise on possible aliasing
-        // (100.4 ms).
-        dense_rows_te(acc, ld, a.dense_rs, a.dense_cs, a.dchunk_off, a.dchunk_list, a.sp, nsrow, hw,
-                      cpa, last, cp_ns, Tdot, inv_vcp, TRf, eTj);
+    if (a.dense_rs || a.dchunk_slots) {
+        rows_te(a.dense_rs == 0, acc, ld, a.dense_rs, a.dense_cs, a.dchunk_off, a.dchunk_list,
+                a.dchunk_slots, a.cj_slots, a.sp, nsrow, hw, cpa, last, cp_ns, Tdot, inv_vcp, TRf,
+                eTj);
     } else {
-        // sparse output: the bath-gas terms (per-row sums subtracted from every species
-        // column of the pattern), then the column sums of rows T and E
+        // sparse output whose pattern fills under half of the chunk lists' slots
+        // (dchunk_slots null; large sparse mechanisms): the bath-gas terms (per-row
+        // sums subtracted from every species column of the pattern), then the
+        // column sums of rows T and E, two passes over the pattern
         for (int k = 0; k < last; ++k) {
             const double v = rd(nsrow, k);
             if (!nonzero(v)) continue;
@@ -643,6 +663,7 @@ __global__ void __launch_bounds__(PJG_BLOCK, KIND == 1 ? PJG_JAC_MINB : (KIND ==
             acc[(int64_t)__ldg(a.cj_slots + 2 * j + 1) * ld] = TRf * sumE + eTj * J0;
         }
     }
+
     // T column of rows T, E and E column of rows T, E
     double dTsum = (cp_ns * Tjinv - dcp_ns) * conc[last];
     double rate_sum = 0.0, sumT = 0.0, sumE1 = 0.0, spec1 = 0.0, dTsum1 = 0.0;

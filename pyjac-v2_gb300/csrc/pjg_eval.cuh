@@ -72,12 +72,14 @@ struct EvalArgs {
     // dense output: slot of (row r, column c) = r * dense_rs + c * dense_cs
     // (0, 0 for a sparse output, whose slots come from the tables)
     int dense_rs, dense_cs;
-    // dense output: for species columns [PJG_DENSE_COLS c, PJG_DENSE_COLS (c + 1)),
-    // entries dchunk_list[dchunk_off[c] .. dchunk_off[c + 1]) = k << 4 | mask, the
-    // species rows k (increasing) with a structurally nonzero entry there, bit q
-    // of mask for column PJG_DENSE_COLS c + q
+    // for species columns [PJG_DENSE_COLS c, PJG_DENSE_COLS (c + 1)), entries
+    // dchunk_list[dchunk_off[c] .. dchunk_off[c + 1]) = k << 4 | mask, the species
+    // rows k (increasing) with a structurally nonzero entry there, bit q of mask
+    // for column PJG_DENSE_COLS c + q; for a sparse output dchunk_slots holds
+    // the four slots of each listed row (-1 outside the pattern)
     const int* dchunk_off;
     const int* dchunk_list;
+    const int4* dchunk_slots;
     // vector-Jacobian product
     const double* v;          // v[s * phi_ss + j * phi_sj]
     double* vjp;              // same layout
