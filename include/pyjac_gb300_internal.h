@@ -42,9 +42,12 @@ struct pjg_tables;
  * device: for packed position p, orig[p] is the mechanism's reaction index
  * and cls[p] the code that evaluates it (0 the elementary class
  * A + B <=> C + D, 1..10 the mass-action patterns, 11..13 the third-body and
- * fall-off patterns, -1 the general code).  orig and cls hold tables->nr
- * entries each. */
-int pjg_reaction_order(const struct pjg_tables* tables, int32_t* orig, int32_t* cls);
+ * fall-off patterns, -1 the general code); flags[p] (if flags is not NULL)
+ * the packed record's flag word, with the packing's marks 1 << 20 ([M]
+ * equals the previous record's) and 1 << 21 (ln [M] formed earlier in that
+ * run).  Each array holds tables->nr entries. */
+int pjg_reaction_order(const struct pjg_tables* tables, int32_t* orig, int32_t* cls,
+                       int32_t* flags);
 int pjg_eval_chunk(struct pjg_mech* mech, int kind, int64_t n, char order, int jac_format,
                    int64_t* states);
 

@@ -70,7 +70,8 @@ SIGNATURES = [
                                        ctypes.POINTER(ctypes.c_double)]),
     ("pjg_math_exp", ctypes.c_int, [_VP, _VP, ctypes.c_int64, _VP]),
     ("pjg_reaction_order", ctypes.c_int,
-     [ctypes.POINTER(PjgTables), ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+     [ctypes.POINTER(PjgTables), ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+      ctypes.POINTER(ctypes.c_int32)]),
     ("pjg_eval_chunk", ctypes.c_int,
      [_VP, ctypes.c_int, ctypes.c_int64, ctypes.c_char, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
     ("pjg_read_initial_conditions", ctypes.c_int,

@@ -60,20 +60,24 @@ def _tables_struct(pk):
     return t
 
 
-def reaction_order(mech):
+def reaction_order(mech, with_flags=False):
     """The order in which the device tables hold the mechanism's reactions,
     computed on the host (pjg_reaction_order, no device needed): arrays
     (orig, cls) with orig[p] the mechanism index of packed record p and cls[p]
     the code that evaluates it (0 the elementary class A + B <=> C + D, 1..10
     the mass-action patterns, 11..13 the third-body and fall-off patterns, -1
-    the general code)."""
+    the general code).  with_flags=True adds the packed records' flag words
+    (the packing's [M]-reuse marks RX_SAMEM = 1 << 20, RX_SAMELNM = 1 << 21
+    included)."""
     pk = PackedTables(mech)
     t = _tables_struct(pk)
     orig = np.zeros(pk.nr, dtype=np.int32)
     cls = np.zeros(pk.nr, dtype=np.int32)
+    flags = np.zeros(pk.nr, dtype=np.int32)
     _lib.check("pjg_reaction_order", _lib.load().pjg_reaction_order(
-        ctypes.byref(t), orig.ctypes.data_as(_lib._I32P), cls.ctypes.data_as(_lib._I32P)))
-    return orig, cls
+        ctypes.byref(t), orig.ctypes.data_as(_lib._I32P), cls.ctypes.data_as(_lib._I32P),
+        flags.ctypes.data_as(_lib._I32P)))
+    return (orig, cls, flags) if with_flags else (orig, cls)
 
 
 class DeviceMechanism(object):

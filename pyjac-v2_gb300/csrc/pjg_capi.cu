@@ -1064,7 +1064,7 @@ int pjg_mech_destroy(pjg_mech* m)
     return 0;
 }
 
-int pjg_reaction_order(const pjg_tables* tb, int32_t* orig, int32_t* cls)
+int pjg_reaction_order(const pjg_tables* tb, int32_t* orig, int32_t* cls, int32_t* flags)
 {
     if (!tb || tb->nr < 0 || (tb->nr > 0 && (!tb->rxn || !orig || !cls)))
         return fail(PJG_ERR_ARG, "invalid tables or null output");
@@ -1081,6 +1081,7 @@ int pjg_reaction_order(const pjg_tables* tb, int32_t* orig, int32_t* cls)
     for (int p = 0; p < tb->nr; ++p) {
         orig[p] = pk.orig[p];
         cls[p] = pk.cls[p];
+        if (flags) flags[p] = pk.rx[p].flags;
     }
     return 0;
 }

@@ -119,3 +119,42 @@ def test_gri30_group_sizes():
     assert int(((cls >= 1) & (cls <= 10)).sum()) == 41
     assert int(((cls >= 11) & (cls <= 13)).sum()) == 41
     assert int((cls == -1).sum()) == 11
+
+
+RX_SAMEM, RX_SAMELNM = 1 << 20, 1 << 21
+
+
+@pytest.mark.parametrize("name", ["h2o2", "gri30", "testmech", "synthetic_small"])
+def test_third_body_reuse_marks(name):
+    """RX_SAMEM marks a record whose [M] equals the previous record's (same
+    third-body list key, same group), RX_SAMELNM one whose run of such records
+    has already formed ln [M] (an earlier Troe or SRI fall-off whose two rate
+    constants are both of the exponential form); the kernels reuse [M] and
+    ln [M] exactly there."""
+    mech = load_mech(name)
+    orig, cls, flags = pkg("api").reaction_order(mech, with_flags=True)
+    tables = pkg("pack").PackedTables(mech)
+    key = third_body_keys(tables)
+    run_log = False
+    for q in range(len(orig)):
+        f = int(flags[q])
+        same = (q > 0 and key[orig[q]] >= 0 and key[orig[q]] == key[orig[q - 1]]
+                and cls[q] == cls[q - 1])
+        if not same:
+            run_log = False
+        assert bool(f & RX_SAMEM) == same
+        assert bool(f & RX_SAMELNM) == (same and run_log)
+        blend, thd = (f >> 6) & 3, (f >> 4) & 3
+        if thd and blend in (2, 3) and f & 7 == 2 and (f >> 9) & 3 == 2:
+            run_log = True
+        # the marks aside, the flag word is the record's own
+        assert f & ~(RX_SAMEM | RX_SAMELNM) == int(tables.rxn[orig[q]]["flags"])
+
+
+def test_gri30_shares_third_body_concentrations():
+    """GRI-Mech 3.0: 41 third-body and fall-off reactions, 11 distinct [M];
+    the packing forms [M] for fewer than half of them."""
+    orig, cls, flags = pkg("api").reaction_order(load_mech("gri30"), with_flags=True)
+    thd = ((flags >> 4) & 3) != 0
+    assert int(thd.sum()) == 41
+    assert int((thd & ((flags & RX_SAMEM) == 0)).sum()) < 20
